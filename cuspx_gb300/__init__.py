@@ -1,0 +1,329 @@
+"""cuspx_gb300 -- GB300-native SPHINCS+ signing and verification engine.
+
+Python face of the C ABI in include/cuspx.h (the product is the native
+library lib/libcuspx.so; this module only binds it with ctypes).  There is
+no CPU fallback: importing the engine without its built library raises.
+
+    from cuspx_gb300 import Engine
+    eng = Engine()                                   # device 0
+    s = eng.set_id("sha256-128f-simple")
+    pks, sks = eng.keypair_batch(s, seeds)           # seeds: list of 3n-byte strings
+    sigs, status = eng.sign_batch(s, sks, msgs)      # one sk per message
+    verdicts = eng.verify_batch(s, pks, msgs, sigs)  # 0 accept / -1 reject
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(_HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libcuspx.so")
+
+OP_KEYGEN, OP_SIGN, OP_VERIFY = 0, 1, 2
+
+EXPORTS = [
+    "cuspx_num_sets", "cuspx_set_id", "cuspx_set_name", "cuspx_set_sizes", "cuspx_create", "cuspx_destroy",
+    "cuspx_error", "cuspx_set_tuning", "cuspx_get_tuning", "cuspx_keypair_batch", "cuspx_sign_batch",
+    "cuspx_verify_batch", "cuspx_batch_create", "cuspx_batch_destroy", "cuspx_batch_upload", "cuspx_batch_run",
+    "cuspx_batch_download", "cuspx_batch_sync", "cuspx_batch_last_ms", "cuspx_batch_stream",
+    "cuspx_batch_device_ptrs", "cuspx_batch_profile", "cuspx_batch_kernel_ms",
+    "cuspx_randombytes_init", "cuspx_randombytes", "cuspx_aes256_ecb", "cuspx_set_deterministic",
+    "cuspx_deterministic", "cuspx_int_peak",
+]
+
+
+class CuspxError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load lib/libcuspx.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("cuspx_gb300: %s is missing; build it with `python -m cuspx_gb300.build`" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    c = ctypes
+    vp, sz, u8p, i32p, u64p, u32p = c.c_void_p, c.c_size_t, c.c_char_p, c.c_void_p, c.c_void_p, c.c_void_p
+    L.cuspx_set_id.argtypes = [c.c_char_p]
+    L.cuspx_set_name.argtypes = [c.c_int]
+    L.cuspx_set_name.restype = c.c_char_p
+    L.cuspx_set_sizes.argtypes = [c.c_int] + [c.POINTER(c.c_size_t)] * 4 + [c.POINTER(c.c_int)]
+    L.cuspx_create.argtypes = [c.c_int, c.POINTER(vp)]
+    L.cuspx_destroy.argtypes = [vp]
+    L.cuspx_destroy.restype = None
+    L.cuspx_error.argtypes = [vp]
+    L.cuspx_error.restype = c.c_char_p
+    L.cuspx_set_tuning.argtypes = [vp, c.c_int, c.c_int, c.c_int, c.c_int, c.c_int]
+    L.cuspx_get_tuning.argtypes = [vp, c.c_int] + [c.POINTER(c.c_int)] * 4
+    L.cuspx_keypair_batch.argtypes = [vp, c.c_int, sz, vp, vp, vp]
+    L.cuspx_sign_batch.argtypes = [vp, c.c_int, sz, vp, vp, vp, vp, vp, vp, vp]
+    L.cuspx_verify_batch.argtypes = [vp, c.c_int, sz, vp, vp, vp, vp, vp, vp, vp]
+    L.cuspx_batch_create.argtypes = [vp, c.c_int, c.c_int, sz, sz, sz, c.POINTER(vp)]
+    L.cuspx_batch_destroy.argtypes = [vp]
+    L.cuspx_batch_destroy.restype = None
+    L.cuspx_batch_upload.argtypes = [vp, sz, vp, sz, vp, vp, sz, vp, vp, vp, vp]
+    L.cuspx_batch_run.argtypes = [vp]
+    L.cuspx_batch_download.argtypes = [vp, vp, vp, vp]
+    L.cuspx_batch_sync.argtypes = [vp]
+    L.cuspx_batch_last_ms.argtypes = [vp, c.POINTER(c.c_float)]
+    L.cuspx_batch_stream.argtypes = [vp]
+    L.cuspx_batch_stream.restype = vp
+    L.cuspx_batch_device_ptrs.argtypes = [vp] + [c.POINTER(vp)] * 7
+    L.cuspx_batch_profile.argtypes = [vp, c.c_int]
+    L.cuspx_batch_kernel_ms.argtypes = [vp, c.c_int, c.POINTER(c.c_char_p), c.POINTER(c.c_double),
+                                        c.POINTER(c.c_long)]
+    L.cuspx_randombytes_init.argtypes = [vp, vp, c.c_int]
+    L.cuspx_randombytes_init.restype = None
+    L.cuspx_randombytes.argtypes = [vp, c.c_ulonglong]
+    L.cuspx_aes256_ecb.argtypes = [vp, vp, vp]
+    L.cuspx_aes256_ecb.restype = None
+    L.cuspx_set_deterministic.argtypes = [c.c_int]
+    L.cuspx_set_deterministic.restype = None
+    L.cuspx_int_peak.argtypes = [c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
+    _lib = L
+    return L
+
+
+def _buf(b):
+    """ctypes pointer to the bytes of b (bytes / bytearray / numpy array)."""
+    if b is None:
+        return None
+    if isinstance(b, bytes):
+        return ctypes.cast(ctypes.c_char_p(b), ctypes.c_void_p)
+    try:
+        import numpy as np
+        if isinstance(b, np.ndarray):
+            assert b.flags["C_CONTIGUOUS"]
+            return ctypes.c_void_p(b.ctypes.data)
+    except ImportError:
+        pass
+    if isinstance(b, (bytearray, memoryview)):
+        return ctypes.cast((ctypes.c_char * len(b)).from_buffer(b), ctypes.c_void_p)
+    if isinstance(b, ctypes.Array):
+        return ctypes.cast(b, ctypes.c_void_p)
+    raise TypeError("unsupported buffer %r" % type(b))
+
+
+def num_sets():
+    return lib().cuspx_num_sets()
+
+
+def set_id(name):
+    r = lib().cuspx_set_id(name.encode())
+    if r < 0:
+        raise ValueError("unknown parameter set %r" % name)
+    return r
+
+
+def set_name(sid):
+    return lib().cuspx_set_name(sid).decode()
+
+
+def set_sizes(sid):
+    """dict(pk, sk, sig, seed, n) in bytes"""
+    v = [ctypes.c_size_t() for _ in range(4)]
+    n = ctypes.c_int()
+    if lib().cuspx_set_sizes(sid, *[ctypes.byref(x) for x in v], ctypes.byref(n)) != 0:
+        raise ValueError("bad set id %r" % sid)
+    return dict(pk=v[0].value, sk=v[1].value, sig=v[2].value, seed=v[3].value, n=n.value)
+
+
+def pack_messages(msgs):
+    """Messages -> (slab bytes, offsets, lengths) with 16-byte aligned offsets."""
+    import numpy as np
+    lens = np.array([len(m) for m in msgs], dtype=np.uint64)
+    offs = np.zeros(len(msgs), dtype=np.uint64)
+    total = 0
+    for i, m in enumerate(msgs):
+        offs[i] = total
+        total += (len(m) + 15) & ~15
+    slab = bytearray(total + 16)
+    for i, m in enumerate(msgs):
+        o = int(offs[i])
+        slab[o:o + len(m)] = m
+    return slab, offs, lens
+
+
+class Engine:
+    """One device context (cuspx_create)."""
+
+    def __init__(self, device=0):
+        self.L = lib()
+        h = ctypes.c_void_p()
+        rc = self.L.cuspx_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise CuspxError("cuspx_create(%d) failed (%d): no usable CUDA device" % (device, rc))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.cuspx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise CuspxError("%s failed (%d): %s" % (what, rc, self.L.cuspx_error(self.h).decode()))
+
+    set_id = staticmethod(set_id)
+    set_sizes = staticmethod(set_sizes)
+
+    def set_tuning(self, sid, leaf_block=0, fors_block=0, verify_block=0, tree_warps=0):
+        self._check(self.L.cuspx_set_tuning(self.h, sid, leaf_block, fors_block, verify_block, tree_warps),
+                    "set_tuning")
+
+    def get_tuning(self, sid):
+        v = [ctypes.c_int() for _ in range(4)]
+        self._check(self.L.cuspx_get_tuning(self.h, sid, *[ctypes.byref(x) for x in v]), "get_tuning")
+        return dict(leaf_block=v[0].value, fors_block=v[1].value, verify_block=v[2].value, tree_warps=v[3].value)
+
+    def keypair_batch(self, sid, seeds):
+        z = set_sizes(sid)
+        cnt = len(seeds)
+        sb = b"".join(bytes(s) for s in seeds)
+        assert len(sb) == cnt * z["seed"]
+        pk = ctypes.create_string_buffer(cnt * z["pk"])
+        sk = ctypes.create_string_buffer(cnt * z["sk"])
+        self._check(self.L.cuspx_keypair_batch(self.h, sid, cnt, _buf(sb), _buf(pk), _buf(sk)), "keypair_batch")
+        return ([pk.raw[i * z["pk"]:(i + 1) * z["pk"]] for i in range(cnt)],
+                [sk.raw[i * z["sk"]:(i + 1) * z["sk"]] for i in range(cnt)])
+
+    def sign_batch(self, sid, sks, msgs, optrand=None):
+        import numpy as np
+        z = set_sizes(sid)
+        cnt = len(msgs)
+        assert len(sks) == cnt
+        skb = b"".join(bytes(s) for s in sks)
+        slab, offs, lens = pack_messages(msgs)
+        opt = b"".join(bytes(o) for o in optrand) if optrand is not None else None
+        sig = ctypes.create_string_buffer(max(1, cnt * z["sig"]))
+        st = np.zeros(cnt, dtype=np.int32)
+        self._check(self.L.cuspx_sign_batch(self.h, sid, cnt, _buf(skb), _buf(slab), _buf(offs), _buf(lens),
+                                            _buf(opt), _buf(sig), _buf(st)), "sign_batch")
+        return [sig.raw[i * z["sig"]:(i + 1) * z["sig"]] for i in range(cnt)], st
+
+    def verify_batch(self, sid, pks, msgs, sigs, siglens=None):
+        import numpy as np
+        z = set_sizes(sid)
+        cnt = len(msgs)
+        pkb = b"".join(bytes(p) for p in pks)
+        slab, offs, lens = pack_messages(msgs)
+        rows = bytearray(cnt * z["sig"])
+        sl = np.zeros(cnt, dtype=np.uint64)
+        for i, s in enumerate(sigs):
+            s = bytes(s)[:z["sig"]]
+            rows[i * z["sig"]:i * z["sig"] + len(s)] = s
+            sl[i] = len(sigs[i]) if siglens is None else siglens[i]
+        v = np.zeros(cnt, dtype=np.int32)
+        self._check(self.L.cuspx_verify_batch(self.h, sid, cnt, _buf(pkb), _buf(slab), _buf(offs), _buf(lens),
+                                              _buf(rows), _buf(sl), _buf(v)), "verify_batch")
+        return v
+
+    def batch(self, op, sid, capacity, msg_capacity=0, key_capacity=0):
+        return Batch(self, op, sid, capacity, msg_capacity, key_capacity)
+
+
+class Batch:
+    """A reusable device-resident batch (cuspx_batch_*)."""
+
+    def __init__(self, eng, op, sid, capacity, msg_capacity=0, key_capacity=0):
+        self.eng, self.L, self.op, self.sid = eng, eng.L, op, sid
+        self.sizes = set_sizes(sid)
+        h = ctypes.c_void_p()
+        eng._check(self.L.cuspx_batch_create(eng.h, op, sid, capacity, msg_capacity, key_capacity,
+                                              ctypes.byref(h)), "batch_create")
+        self.h = h
+        self.count = 0
+
+    def close(self):
+        if self.h:
+            self.L.cuspx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, count, keys, nkeys=0, key_index=None, msgs=None, msg_bytes=0, msg_off=None, msg_len=None,
+               aux=None, siglens=None):
+        self.eng._check(self.L.cuspx_batch_upload(self.h, count, _buf(keys), nkeys, _buf(key_index), _buf(msgs),
+                                                  msg_bytes, _buf(msg_off), _buf(msg_len), _buf(aux),
+                                                  _buf(siglens)), "batch_upload")
+        self.count = count
+
+    def run(self):
+        self.eng._check(self.L.cuspx_batch_run(self.h), "batch_run")
+
+    def download(self, out=None, out2=None, status=None):
+        self.eng._check(self.L.cuspx_batch_download(self.h, _buf(out), _buf(out2), _buf(status)), "batch_download")
+
+    def sync(self):
+        self.eng._check(self.L.cuspx_batch_sync(self.h), "batch_sync")
+
+    def last_ms(self):
+        f = ctypes.c_float()
+        self.eng._check(self.L.cuspx_batch_last_ms(self.h, ctypes.byref(f)), "batch_last_ms")
+        return f.value
+
+    def stream(self):
+        return self.L.cuspx_batch_stream(self.h)
+
+    def profile(self, enable=True):
+        self.eng._check(self.L.cuspx_batch_profile(self.h, 1 if enable else 0), "batch_profile")
+
+    def kernel_ms(self):
+        n = self.L.cuspx_batch_kernel_ms(self.h, -1, None, None, None)
+        out = []
+        for i in range(n):
+            name = ctypes.c_char_p()
+            ms = ctypes.c_double()
+            cnt = ctypes.c_long()
+            self.L.cuspx_batch_kernel_ms(self.h, i, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(cnt))
+            out.append((name.value.decode(), ms.value, cnt.value))
+        return out
+
+
+def randombytes_init(entropy48, personalization=None):
+    lib().cuspx_randombytes_init(_buf(bytes(entropy48)), _buf(personalization), 256)
+
+
+def randombytes(n):
+    b = ctypes.create_string_buffer(max(1, n))
+    lib().cuspx_randombytes(_buf(b), n)
+    return b.raw[:n]
+
+
+def aes256_ecb(key, block):
+    out = ctypes.create_string_buffer(16)
+    lib().cuspx_aes256_ecb(_buf(bytes(key)), _buf(bytes(block)), _buf(out))
+    return out.raw
+
+
+def set_deterministic(on):
+    lib().cuspx_set_deterministic(1 if on else 0)
+
+
+def int_peak(device=0, iters=4096):
+    """Measured integer-ALU peak (ops/s) for the SHF/LOP3/IADD3 mix."""
+    ops = ctypes.c_double()
+    ms = ctypes.c_float()
+    rc = lib().cuspx_int_peak(device, iters, ctypes.byref(ops), ctypes.byref(ms))
+    if rc != 0:
+        raise CuspxError("cuspx_int_peak failed (%d)" % rc)
+    return ops.value, ms.value
+
+
+def dropin_path(set_name):
+    """Path of the NIST api.h drop-in library for one parameter set."""
+    return os.path.join(LIB_DIR, "libspx_%s.so" % set_name)

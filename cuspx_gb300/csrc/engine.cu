@@ -1,0 +1,632 @@
+// engine.cu -- host engine behind include/cuspx.h.
+//
+// Owns contexts (one device each), reusable device-resident batches with
+// their own stream and CUDA graph, and the one-shot host-buffer calls.  The
+// reference's equivalents (face_* launchers in sign.cu) cudaMalloc, copy,
+// launch cooperatively, synchronise and free on every call; here buffers
+// persist per batch and the launch sequence is a replayed CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cuspx.h"
+#include "spx_launch.cuh"
+#include "spx_sets.h"
+
+namespace cuspx {
+FamilyOps g_family[2][3][2];
+void register_family_0_16_0();
+void register_family_0_16_1();
+void register_family_0_24_0();
+void register_family_0_24_1();
+void register_family_0_32_0();
+void register_family_0_32_1();
+void register_family_1_16_0();
+void register_family_1_16_1();
+void register_family_1_24_0();
+void register_family_1_24_1();
+void register_family_1_32_0();
+void register_family_1_32_1();
+
+static std::once_flag g_reg_once;
+static void register_all() {
+    std::call_once(g_reg_once, [] {
+        register_family_0_16_0(); register_family_0_16_1();
+        register_family_0_24_0(); register_family_0_24_1();
+        register_family_0_32_0(); register_family_0_32_1();
+        register_family_1_16_0(); register_family_1_16_1();
+        register_family_1_24_0(); register_family_1_24_1();
+        register_family_1_32_0(); register_family_1_32_1();
+    });
+}
+
+SetParams make_params(const SetDesc &s) {
+    SetParams P;
+    P.n = s.n; P.h = s.h; P.d = s.d; P.hp = s.h / s.d; P.a = s.a; P.k = s.k;
+    P.len1 = 2 * s.n;
+    P.len2 = 3;
+    P.len = P.len1 + P.len2;
+    P.fors_msg_bytes = (s.a * s.k + 7) / 8;
+    P.fors_bytes = (s.a + 1) * s.k * s.n;
+    P.wots_bytes = P.len * s.n;
+    P.sig_bytes = s.n + P.fors_bytes + s.d * P.wots_bytes + s.h * s.n;
+    P.tree_bits = P.hp * (s.d - 1);
+    P.tree_bytes = (P.tree_bits + 7) / 8;
+    P.leaf_bits = P.hp;
+    P.leaf_bytes = (P.leaf_bits + 7) / 8;
+    P.dgst_bytes = P.fors_msg_bytes + P.tree_bytes + P.leaf_bytes;
+    P.pk_bytes = 2 * s.n;
+    P.sk_bytes = 4 * s.n;
+    return P;
+}
+
+static const FamilyOps &family_of(int set) {
+    const SetDesc &s = kSets[set];
+    return g_family[s.hash][s.n / 8 - 2][s.robust];
+}
+}  // namespace cuspx
+
+using namespace cuspx;
+
+struct cuspx_ctx {
+    int device = 0;
+    std::string err;
+    Tuning tune[kNumSets];
+    bool configured[2][3][2] = {};
+    std::mutex mu;
+    cuspx_batch *oneshot[3][kNumSets] = {};
+};
+
+struct ProfEntry {
+    const char *name;
+    double ms;
+    long launches;
+};
+
+struct cuspx_batch {
+    cuspx_ctx *ctx = nullptr;
+    int op = 0, set = 0;
+    SetParams P{};
+    size_t cap = 0, msg_cap = 0, key_cap = 0;
+    cudaStream_t s = nullptr;
+    uint8_t *keys = nullptr;
+    uint32_t *keyrow = nullptr;
+    uint8_t *msg = nullptr;
+    uint64_t *off = nullptr, *len = nullptr;
+    uint8_t *aux = nullptr;
+    uint64_t *siglen = nullptr;
+    uint8_t *out = nullptr;
+    int32_t *status = nullptr;
+    SignWork *work = nullptr;
+    uint8_t *fors_roots = nullptr, *leaves = nullptr, *roots = nullptr, *chains = nullptr;
+    size_t count = 0;
+    bool use_keyrow = false, use_aux = false, use_siglen = false;
+    cudaGraphExec_t gexec = nullptr;
+    size_t g_count = 0;
+    bool g_keyrow = false, g_aux = false, g_siglen = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool ran = false;
+    bool profile = false;
+    bool prof_pending = false;
+    PhaseTimer pt;
+    std::vector<ProfEntry> prof;
+    std::vector<void *> allocs;
+};
+
+static int fail(cuspx_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+static int cuda_fail(cuspx_ctx *ctx, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(ctx, CUSPX_ENOMEM, m);
+    return fail(ctx, CUSPX_ECUDA, m);
+}
+
+#define CK(call, ctx)                                         \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, #call); \
+    } while (0)
+
+extern "C" {
+
+int cuspx_num_sets(void) { return kNumSets; }
+
+int cuspx_set_id(const char *name) {
+    if (!name) return CUSPX_EINVAL;
+    int id = set_by_name(name);
+    return id < 0 ? CUSPX_EINVAL : id;
+}
+
+const char *cuspx_set_name(int set) {
+    if (set < 0 || set >= kNumSets) return nullptr;
+    return kSets[set].name;
+}
+
+int cuspx_set_sizes(int set, size_t *pk, size_t *sk, size_t *sig, size_t *seed, int *n) {
+    if (set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    SetParams P = make_params(kSets[set]);
+    if (pk) *pk = P.pk_bytes;
+    if (sk) *sk = P.sk_bytes;
+    if (sig) *sig = P.sig_bytes;
+    if (seed) *seed = 3 * P.n;
+    if (n) *n = P.n;
+    return CUSPX_OK;
+}
+
+int cuspx_create(int device, cuspx_ctx **out) {
+    if (!out) return CUSPX_EINVAL;
+    *out = nullptr;
+    register_all();
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) return CUSPX_ECUDA;
+    cuspx_ctx *c = new cuspx_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete c;
+        return CUSPX_ECUDA;
+    }
+    *out = c;
+    return CUSPX_OK;
+}
+
+void cuspx_destroy(cuspx_ctx *ctx) {
+    if (!ctx) return;
+    for (auto &row : ctx->oneshot)
+        for (auto *b : row)
+            if (b) cuspx_batch_destroy(b);
+    delete ctx;
+}
+
+const char *cuspx_error(const cuspx_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int cuspx_set_tuning(cuspx_ctx *ctx, int set, int leaf_block, int fors_block, int verify_block, int tree_warps) {
+    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    Tuning &t = ctx->tune[set];
+    if (leaf_block > 0) {
+        if (leaf_block % 32 || leaf_block > 1024) return fail(ctx, CUSPX_EINVAL, "leaf_block must be a multiple of 32 <= 1024");
+        t.leaf_block = leaf_block;
+    }
+    if (fors_block > 0) {
+        if (fors_block % 32 || fors_block > 1024) return fail(ctx, CUSPX_EINVAL, "fors_block must be a multiple of 32 <= 1024");
+        t.fors_block = fors_block;
+    }
+    if (verify_block > 0) {
+        if (verify_block % 32 || verify_block > 1024) return fail(ctx, CUSPX_EINVAL, "verify_block must be a multiple of 32 <= 1024");
+        t.verify_block = verify_block;
+    }
+    if (tree_warps > 0) {
+        if (tree_warps > 32) return fail(ctx, CUSPX_EINVAL, "tree_warps must be <= 32");
+        t.tree_warps = tree_warps;
+    }
+    return CUSPX_OK;
+}
+
+int cuspx_get_tuning(cuspx_ctx *ctx, int set, int *leaf_block, int *fors_block, int *verify_block, int *tree_warps) {
+    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    const Tuning &t = ctx->tune[set];
+    if (leaf_block) *leaf_block = t.leaf_block;
+    if (fors_block) *fors_block = t.fors_block;
+    if (verify_block) *verify_block = t.verify_block;
+    if (tree_warps) *tree_warps = t.tree_warps;
+    return CUSPX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+static int balloc(cuspx_batch *b, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return CUSPX_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(b->ctx, e, "cudaMalloc");
+    }
+    b->allocs.push_back(*p);
+    return CUSPX_OK;
+}
+
+int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t msg_capacity, size_t key_capacity,
+                       cuspx_batch **out) {
+    if (!ctx || !out || set < 0 || set >= kNumSets || op < 0 || op > 2 || capacity == 0 || capacity > (1u << 30))
+        return fail(ctx, CUSPX_EINVAL, "batch_create: bad argument");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device), ctx);
+    const SetDesc &sd = kSets[set];
+    FamilyOps &ops = g_family[sd.hash][sd.n / 8 - 2][sd.robust];
+    if (!ctx->configured[sd.hash][sd.n / 8 - 2][sd.robust]) {
+        CK(ops.configure(), ctx);
+        ctx->configured[sd.hash][sd.n / 8 - 2][sd.robust] = true;
+    }
+    cuspx_batch *b = new cuspx_batch();
+    b->ctx = ctx;
+    b->op = op;
+    b->set = set;
+    b->P = make_params(sd);
+    b->cap = capacity;
+    b->msg_cap = msg_capacity;
+    b->key_cap = key_capacity ? key_capacity : capacity;
+    const SetParams &P = b->P;
+    const size_t n = P.n, cap = capacity;
+    int rc = CUSPX_OK;
+    auto A = [&](void **p, size_t bytes) {
+        if (rc == CUSPX_OK) rc = balloc(b, p, bytes);
+    };
+    if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return fail(ctx, CUSPX_ECUDA, "cudaStreamCreate");
+    }
+    cudaEventCreate(&b->e0);
+    cudaEventCreate(&b->e1);
+    for (auto &e : b->pt.ev) cudaEventCreate(&e);
+    const size_t keyrow_bytes = op == CUSPX_OP_VERIFY ? 2 * n : 4 * n;
+    A((void **)&b->keys, b->key_cap * keyrow_bytes);
+    A((void **)&b->status, cap * sizeof(int32_t));
+    if (op == CUSPX_OP_KEYGEN) {
+        A((void **)&b->out, cap * 2 * n);
+        A((void **)&b->leaves, cap * ((size_t)1 << P.hp) * n);
+        A((void **)&b->roots, cap * n);
+    } else {
+        A((void **)&b->keyrow, cap * sizeof(uint32_t));
+        A((void **)&b->msg, msg_capacity + 64);
+        A((void **)&b->off, cap * sizeof(uint64_t));
+        A((void **)&b->len, cap * sizeof(uint64_t));
+        A((void **)&b->work, cap * sizeof(SignWork));
+        A((void **)&b->fors_roots, cap * P.k * n);
+        if (op == CUSPX_OP_SIGN) {
+            A((void **)&b->aux, cap * n);
+            A((void **)&b->out, cap * P.sig_bytes);
+            A((void **)&b->leaves, cap * P.d * ((size_t)1 << P.hp) * n);
+            A((void **)&b->roots, cap * P.d * n);
+            A((void **)&b->chains, cap * P.d * P.len * 16 * n);
+        } else {
+            A((void **)&b->aux, cap * P.sig_bytes);
+            A((void **)&b->siglen, cap * sizeof(uint64_t));
+        }
+    }
+    if (rc != CUSPX_OK) {
+        std::string m = ctx->err;
+        cuspx_batch_destroy(b);
+        ctx->err = m;
+        return rc;
+    }
+    *out = b;
+    return CUSPX_OK;
+}
+
+void cuspx_batch_destroy(cuspx_batch *b) {
+    if (!b) return;
+    if (b->s) cudaStreamSynchronize(b->s);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (void *p : b->allocs) cudaFree(p);
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    for (auto &e : b->pt.ev)
+        if (e) cudaEventDestroy(e);
+    if (b->s) cudaStreamDestroy(b->s);
+    delete b;
+}
+
+int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t nkeys, const uint32_t *key_index,
+                       const uint8_t *msgs, size_t msg_bytes, const uint64_t *msg_off, const uint64_t *msg_len,
+                       const uint8_t *aux, const uint64_t *siglens) {
+    if (!b) return CUSPX_EINVAL;
+    cuspx_ctx *ctx = b->ctx;
+    const SetParams &P = b->P;
+    const size_t n = P.n;
+    if (count > b->cap) return fail(ctx, CUSPX_EINVAL, "upload: count exceeds batch capacity");
+    if (count && !keys) return fail(ctx, CUSPX_EINVAL, "upload: keys is null");
+    CK(cudaSetDevice(ctx->device), ctx);
+    if (b->op == CUSPX_OP_KEYGEN) {
+        // seeds (count x 3n) into the first 3n bytes of each sk row
+        if (count) CK(cudaMemcpy2DAsync(b->keys, 4 * n, keys, 3 * n, 3 * n, count, cudaMemcpyHostToDevice, b->s), ctx);
+        b->count = count;
+        return CUSPX_OK;
+    }
+    if (nkeys == 0) nkeys = count;
+    if (nkeys > b->key_cap) return fail(ctx, CUSPX_EINVAL, "upload: more keys than key capacity");
+    if (key_index) {
+        for (size_t i = 0; i < count; i++)
+            if (key_index[i] >= nkeys) return fail(ctx, CUSPX_EINVAL, "upload: key_index out of range");
+    } else if (nkeys < count) {
+        return fail(ctx, CUSPX_EINVAL, "upload: fewer keys than items and no key_index");
+    }
+    if (count && (!msg_off || !msg_len)) return fail(ctx, CUSPX_EINVAL, "upload: message offsets/lengths are null");
+    for (size_t i = 0; i < count; i++) {
+        if (msg_off[i] % 16) return fail(ctx, CUSPX_EINVAL, "upload: message offsets must be multiples of 16");
+        if (msg_off[i] + msg_len[i] > msg_bytes || msg_off[i] + msg_len[i] < msg_off[i])
+            return fail(ctx, CUSPX_EINVAL, "upload: message outside the message buffer");
+    }
+    if (msg_bytes > b->msg_cap) return fail(ctx, CUSPX_EINVAL, "upload: messages exceed message capacity");
+    const size_t krow = b->op == CUSPX_OP_VERIFY ? 2 * n : 4 * n;
+    if (nkeys) CK(cudaMemcpyAsync(b->keys, keys, nkeys * krow, cudaMemcpyHostToDevice, b->s), ctx);
+    if (key_index && count) CK(cudaMemcpyAsync(b->keyrow, key_index, count * 4, cudaMemcpyHostToDevice, b->s), ctx);
+    if (msg_bytes) CK(cudaMemcpyAsync(b->msg, msgs, msg_bytes, cudaMemcpyHostToDevice, b->s), ctx);
+    if (count) {
+        CK(cudaMemcpyAsync(b->off, msg_off, count * 8, cudaMemcpyHostToDevice, b->s), ctx);
+        CK(cudaMemcpyAsync(b->len, msg_len, count * 8, cudaMemcpyHostToDevice, b->s), ctx);
+    }
+    b->use_keyrow = key_index != nullptr;
+    if (b->op == CUSPX_OP_SIGN) {
+        b->use_aux = aux != nullptr;
+        if (aux && count) CK(cudaMemcpyAsync(b->aux, aux, count * n, cudaMemcpyHostToDevice, b->s), ctx);
+    } else {
+        if (count && !aux) return fail(ctx, CUSPX_EINVAL, "upload: signatures are null");
+        if (count) CK(cudaMemcpyAsync(b->aux, aux, count * P.sig_bytes, cudaMemcpyHostToDevice, b->s), ctx);
+        b->use_siglen = siglens != nullptr;
+        if (siglens && count) CK(cudaMemcpyAsync(b->siglen, siglens, count * 8, cudaMemcpyHostToDevice, b->s), ctx);
+    }
+    b->count = count;
+    return CUSPX_OK;
+}
+
+static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
+    const FamilyOps &ops = family_of(b->set);
+    const Tuning &tu = b->ctx->tune[b->set];
+    const SetParams &P = b->P;
+    const uint32_t cnt = (uint32_t)b->count;
+    if (b->op == CUSPX_OP_SIGN) {
+        SignArgs A;
+        A.count = cnt;
+        A.sk = KeyRef{b->keys, b->use_keyrow ? b->keyrow : nullptr, (uint32_t)P.sk_bytes};
+        A.msg = MsgRef{b->msg, b->off, b->len};
+        A.optrand = b->use_aux ? b->aux : nullptr;
+        A.sig = b->out;
+        A.work = b->work;
+        A.fors_roots = b->fors_roots;
+        A.leaves = b->leaves;
+        A.roots = b->roots;
+        A.chains = b->chains;
+        A.status = b->status;
+        ops.sign(P, A, tu, b->s, pt);
+    } else if (b->op == CUSPX_OP_VERIFY) {
+        VerifyArgs A;
+        A.count = cnt;
+        A.pk = KeyRef{b->keys, b->use_keyrow ? b->keyrow : nullptr, (uint32_t)P.pk_bytes};
+        A.msg = MsgRef{b->msg, b->off, b->len};
+        A.sig = b->aux;
+        A.sig_stride = P.sig_bytes;
+        A.siglen = b->use_siglen ? b->siglen : nullptr;
+        A.work = b->work;
+        A.fors_roots = b->fors_roots;
+        A.verdict = b->status;
+        ops.verify(P, A, tu, b->s, pt);
+    } else {
+        KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots};
+        ops.keygen(P, K, tu, b->s, pt);
+    }
+}
+
+static void collect_profile(cuspx_batch *b) {
+    if (!b->prof_pending) return;
+    b->prof_pending = false;
+    for (int i = 0; i < b->pt.n; i++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->pt.ev[i], b->pt.ev[i + 1]);
+        auto it = std::find_if(b->prof.begin(), b->prof.end(),
+                               [&](const ProfEntry &e) { return !strcmp(e.name, b->pt.names[i]); });
+        if (it == b->prof.end()) b->prof.push_back(ProfEntry{b->pt.names[i], ms, 1});
+        else {
+            it->ms += ms;
+            it->launches++;
+        }
+    }
+}
+
+int cuspx_batch_run(cuspx_batch *b) {
+    if (!b) return CUSPX_EINVAL;
+    cuspx_ctx *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), ctx);
+    if (b->count == 0) return CUSPX_OK;
+    if (b->profile) {
+        collect_profile(b);
+        b->pt.n = 0;
+        CK(cudaEventRecord(b->pt.ev[0], b->s), ctx);
+        CK(cudaEventRecord(b->e0, b->s), ctx);
+        launch_seq(b, &b->pt);
+        CK(cudaGetLastError(), ctx);
+        CK(cudaEventRecord(b->e1, b->s), ctx);
+        b->prof_pending = true;
+        b->ran = true;
+        return CUSPX_OK;
+    }
+    const bool stale = !b->gexec || b->g_count != b->count || b->g_keyrow != b->use_keyrow ||
+                       b->g_aux != b->use_aux || b->g_siglen != b->use_siglen;
+    if (stale) {
+        if (b->gexec) {
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal), ctx);
+        launch_seq(b, nullptr);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(b->s, &g);
+        if (le != cudaSuccess) return cuda_fail(ctx, le, "launch during capture");
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+        b->g_count = b->count;
+        b->g_keyrow = b->use_keyrow;
+        b->g_aux = b->use_aux;
+        b->g_siglen = b->use_siglen;
+    }
+    CK(cudaEventRecord(b->e0, b->s), ctx);
+    CK(cudaGraphLaunch(b->gexec, b->s), ctx);
+    CK(cudaEventRecord(b->e1, b->s), ctx);
+    b->ran = true;
+    return CUSPX_OK;
+}
+
+int cuspx_batch_sync(cuspx_batch *b) {
+    if (!b) return CUSPX_EINVAL;
+    CK(cudaStreamSynchronize(b->s), b->ctx);
+    collect_profile(b);
+    return CUSPX_OK;
+}
+
+int cuspx_batch_download(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status) {
+    if (!b) return CUSPX_EINVAL;
+    cuspx_ctx *ctx = b->ctx;
+    const SetParams &P = b->P;
+    CK(cudaSetDevice(ctx->device), ctx);
+    const size_t cnt = b->count;
+    if (cnt) {
+        if (b->op == CUSPX_OP_SIGN) {
+            if (out) CK(cudaMemcpyAsync(out, b->out, cnt * P.sig_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
+        } else if (b->op == CUSPX_OP_KEYGEN) {
+            if (out) CK(cudaMemcpyAsync(out, b->keys, cnt * P.sk_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
+            if (out2) CK(cudaMemcpyAsync(out2, b->out, cnt * P.pk_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
+        }
+        if (status && b->op != CUSPX_OP_KEYGEN)
+            CK(cudaMemcpyAsync(status, b->status, cnt * 4, cudaMemcpyDeviceToHost, b->s), ctx);
+    }
+    return cuspx_batch_sync(b);
+}
+
+int cuspx_batch_last_ms(cuspx_batch *b, float *ms) {
+    if (!b || !ms || !b->ran) return CUSPX_EINVAL;
+    CK(cudaEventSynchronize(b->e1), b->ctx);
+    CK(cudaEventElapsedTime(ms, b->e0, b->e1), b->ctx);
+    return CUSPX_OK;
+}
+
+void *cuspx_batch_stream(cuspx_batch *b) { return b ? (void *)b->s : nullptr; }
+
+int cuspx_batch_device_ptrs(cuspx_batch *b, void **keys, void **msgs, void **msg_off, void **msg_len, void **aux,
+                            void **out, void **status) {
+    if (!b) return CUSPX_EINVAL;
+    if (keys) *keys = b->keys;
+    if (msgs) *msgs = b->msg;
+    if (msg_off) *msg_off = b->off;
+    if (msg_len) *msg_len = b->len;
+    if (aux) *aux = b->aux;
+    if (out) *out = b->out;
+    if (status) *status = b->status;
+    return CUSPX_OK;
+}
+
+int cuspx_batch_profile(cuspx_batch *b, int enable) {
+    if (!b) return CUSPX_EINVAL;
+    if (b->profile && !enable) cuspx_batch_sync(b);
+    b->profile = enable != 0;
+    if (enable) b->prof.clear();
+    return CUSPX_OK;
+}
+
+int cuspx_batch_kernel_ms(cuspx_batch *b, int idx, const char **name, double *ms, long *launches) {
+    if (!b) return CUSPX_EINVAL;
+    cuspx_batch_sync(b);
+    if (idx < 0) return (int)b->prof.size();
+    if (idx >= (int)b->prof.size()) return CUSPX_EINVAL;
+    if (name) *name = b->prof[idx].name;
+    if (ms) *ms = b->prof[idx].ms;
+    if (launches) *launches = b->prof[idx].launches;
+    return CUSPX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one-shot host-buffer calls
+// ---------------------------------------------------------------------------
+static int oneshot_batch(cuspx_ctx *ctx, int op, int set, size_t count, size_t msg_bytes, cuspx_batch **out) {
+    cuspx_batch *&b = ctx->oneshot[op][set];
+    if (b && (b->cap < count || b->msg_cap < msg_bytes)) {
+        cuspx_batch_destroy(b);
+        b = nullptr;
+    }
+    if (!b) {
+        size_t cap = std::max<size_t>(count, 1);
+        size_t mcap = std::max<size_t>(msg_bytes, 4096);
+        int rc = cuspx_batch_create(ctx, op, set, cap, mcap, cap, &b);
+        if (rc) {
+            b = nullptr;
+            return rc;
+        }
+    }
+    *out = b;
+    return CUSPX_OK;
+}
+
+// pack messages at 16-byte aligned offsets
+static size_t pack_msgs(size_t count, const uint8_t *msgs, const uint64_t *off, const uint64_t *len,
+                        std::vector<uint8_t> &slab, std::vector<uint64_t> &noff) {
+    size_t total = 0;
+    noff.resize(count);
+    for (size_t i = 0; i < count; i++) {
+        noff[i] = total;
+        total += (len[i] + 15) & ~(uint64_t)15;
+    }
+    slab.assign(total + 16, 0);
+    for (size_t i = 0; i < count; i++)
+        if (len[i]) memcpy(slab.data() + noff[i], msgs + off[i], len[i]);
+    return total;
+}
+
+int cuspx_keypair_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *seeds, uint8_t *pks, uint8_t *sks) {
+    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    if (count == 0) return CUSPX_OK;
+    if (!seeds || !pks || !sks) return fail(ctx, CUSPX_EINVAL, "keypair_batch: null buffer");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cuspx_batch *b;
+    int rc = oneshot_batch(ctx, CUSPX_OP_KEYGEN, set, count, 0, &b);
+    if (rc) return rc;
+    if ((rc = cuspx_batch_upload(b, count, seeds, count, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr)))
+        return rc;
+    if ((rc = cuspx_batch_run(b))) return rc;
+    return cuspx_batch_download(b, sks, pks, nullptr);
+}
+
+int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, const uint8_t *msgs,
+                     const uint64_t *msg_off, const uint64_t *msg_len, const uint8_t *optrand, uint8_t *sigs,
+                     int32_t *status) {
+    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    if (count == 0) return CUSPX_OK;
+    if (!sks || !msg_off || !msg_len || !sigs) return fail(ctx, CUSPX_EINVAL, "sign_batch: null buffer");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::vector<uint8_t> slab;
+    std::vector<uint64_t> noff;
+    size_t total = pack_msgs(count, msgs, msg_off, msg_len, slab, noff);
+    cuspx_batch *b;
+    int rc = oneshot_batch(ctx, CUSPX_OP_SIGN, set, count, total, &b);
+    if (rc) return rc;
+    if ((rc = cuspx_batch_upload(b, count, sks, count, nullptr, slab.data(), total, noff.data(), msg_len, optrand,
+                                 nullptr)))
+        return rc;
+    if ((rc = cuspx_batch_run(b))) return rc;
+    std::vector<int32_t> st(count);
+    rc = cuspx_batch_download(b, sigs, nullptr, st.data());
+    if (status) memcpy(status, st.data(), count * 4);
+    return rc;
+}
+
+int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks, const uint8_t *msgs,
+                       const uint64_t *msg_off, const uint64_t *msg_len, const uint8_t *sigs,
+                       const uint64_t *siglens, int32_t *verdicts) {
+    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    if (count == 0) return CUSPX_OK;
+    if (!pks || !msg_off || !msg_len || !sigs || !verdicts) return fail(ctx, CUSPX_EINVAL, "verify_batch: null buffer");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::vector<uint8_t> slab;
+    std::vector<uint64_t> noff;
+    size_t total = pack_msgs(count, msgs, msg_off, msg_len, slab, noff);
+    cuspx_batch *b;
+    int rc = oneshot_batch(ctx, CUSPX_OP_VERIFY, set, count, total, &b);
+    if (rc) return rc;
+    if ((rc = cuspx_batch_upload(b, count, pks, count, nullptr, slab.data(), total, noff.data(), msg_len, sigs,
+                                 siglens)))
+        return rc;
+    if ((rc = cuspx_batch_run(b))) return rc;
+    return cuspx_batch_download(b, nullptr, nullptr, verdicts);
+}
+
+}  // extern "C"

@@ -1,0 +1,667 @@
+// spx_kernels.cuh -- SPHINCS+ keygen / sign / verify kernels, templated on a
+// hash family policy (Sha2<N,R> or Shake<N,R>, spx_thash.cuh).
+//
+// Sign is a fixed pipeline of phase kernels over a batch (captured in a CUDA
+// graph by the host engine).  Every phase is flat over independent work so a
+// batch of thousands of signatures fills all 152 SMs:
+//
+//   k_sign_msg      thread / signature   PRF_msg, H_msg -> R, FORS digest, tree, leaf
+//   k_fors_sign     warp / FORS tree     leaves (PRF+F), per-lane subtree stack,
+//                                        5 shuffle levels, auth path, root
+//   k_leaves        thread / XMSS leaf   WOTS+ key (len chains x 15 F) streamed into
+//                                        T_len; the signing leaf records its chains
+//   k_trees         warp / XMSS tree     level-by-level reduction in shared memory,
+//                                        auth path, root
+//   k_sign_finish   block / signature    FORS pk (T_k), WOTS signatures gathered
+//                                        from the recorded chains
+//
+// Reference structure followed (CPU form): crypto_sign_signature sign.cu:1924-1994,
+// fors_sign fors.cu:107-143, treehash utils.cu:189-241, wots_gen_leaf sign.cu:87-102,
+// wots_sign wots.cu:614-625, crypto_sign_verify sign.cu:3048-3121,
+// crypto_sign_seed_keypair sign.cu:154-182.
+#pragma once
+#include "spx_thash.cuh"
+
+namespace cuspx {
+
+// runtime parameter set (params.h:33-146)
+struct SetParams {
+    int n, h, d, hp, a, k, len, len1, len2;
+    int sig_bytes, fors_bytes, wots_bytes, fors_msg_bytes, dgst_bytes;
+    int tree_bits, tree_bytes, leaf_bits, leaf_bytes;
+    int pk_bytes, sk_bytes;
+};
+
+// per-signature plan produced by the message phase (96 bytes): the FORS
+// digest, hypertree position and the key's SHA-256 midstate, computed once
+// per item instead of once per lane.
+struct SignWork {
+    uint64_t tree;
+    uint32_t idx_leaf;
+    uint32_t flags;
+    uint8_t mhash[48];
+    uint32_t mid[8];
+};
+
+// key registers for an item whose midstate is already in its work record
+template <class HF>
+SPX_DEV void key_from_work(KeyRegs<4 * HF::W> &k, const uint8_t *skseed, const uint8_t *pub, const SignWork &w) {
+    HF::load(k.skseed, skseed);
+    HF::load(k.pub, pub);
+#pragma unroll
+    for (int i = 0; i < 8; i++) k.mid[i] = w.mid[i];
+}
+
+// Key rows: item i uses key bytes keys + keyrow[i] * key_stride (or row i
+// when keyrow is null).  For signing a key row is sk = SK_SEED || SK_PRF ||
+// PUB_SEED || ROOT; for verifying it is pk = PUB_SEED || ROOT.
+struct KeyRef {
+    const uint8_t *keys;
+    const uint32_t *keyrow;
+    uint32_t stride;
+    SPX_DEV const uint8_t *row(uint32_t i) const { return keys + (uint64_t)(keyrow ? keyrow[i] : i) * stride; }
+};
+
+struct MsgRef {
+    const uint8_t *base;       // 16-byte aligned message slab (slack >= 8 bytes past every message)
+    const uint64_t *off;       // per-item byte offset, multiple of 16
+    const uint64_t *len;       // per-item length
+};
+
+struct SignArgs {
+    uint32_t count;
+    KeyRef sk;
+    MsgRef msg;
+    const uint8_t *optrand;    // count x n, or null for the reference's fixed 0xAD.. (sign.cu:1951-1954)
+    uint8_t *sig;              // count x sig_bytes
+    SignWork *work;            // count
+    uint8_t *fors_roots;       // count x k x n
+    uint8_t *leaves;           // count x d x 2^hp x n
+    uint8_t *roots;            // count x d x n
+    uint8_t *chains;           // count x d x len x 16 x n  (signing leaf's chain values)
+    int32_t *status;           // count
+};
+
+// tree/leaf indices of hypertree layer L (sign.cu:1987-1988)
+SPX_DEV void layer_index(const SetParams &P, uint64_t tree, uint32_t idx_leaf, int L, uint64_t &tree_L,
+                         uint32_t &idx_L) {
+    const uint32_t mask = (1u << P.hp) - 1u;
+    if (L == 0) {
+        tree_L = tree;
+        idx_L = idx_leaf;
+    } else {
+        uint64_t t = P.hp * (L - 1) >= 64 ? 0 : (tree >> (P.hp * (L - 1)));
+        idx_L = (uint32_t)(t & mask);
+        tree_L = P.hp >= 64 ? 0 : (t >> P.hp);
+    }
+}
+
+// LSB-first FORS index of tree t (message_to_indices, fors.cu:77-88)
+SPX_DEV uint32_t fors_index(const uint8_t *mh, int a, int t) {
+    uint32_t v = 0;
+    int off = t * a;
+    for (int j = 0; j < a; j++, off++) v |= ((uint32_t)(mh[off >> 3] >> (off & 7)) & 1u) << j;
+    return v;
+}
+
+// WOTS+ chain length for chain c of message msg (chain_lengths, wots.cu:84-166):
+// base-16 digits MSB nibble first, then the checksum sum(15 - d) shifted left
+// by (8 - len2*4 % 8) % 8 and split into len2 digits.
+template <class HF>
+SPX_DEV uint32_t chain_len(const SetParams &P, const uint32_t msg[HF::W], int c) {
+    auto nib = [&](int i) -> uint32_t {
+        // byte i/2 of the value, MSB nibble first
+        uint32_t byte;
+        if (HF::kShake) byte = (msg[i >> 3] >> (8 * ((i >> 1) & 3))) & 0xffu;
+        else byte = (msg[i >> 3] >> (24 - 8 * ((i >> 1) & 3))) & 0xffu;
+        return (i & 1) ? (byte & 15u) : (byte >> 4);
+    };
+    if (c < P.len1) return nib(c);
+    uint32_t csum = 0;
+    for (int i = 0; i < P.len1; i++) csum += 15u - nib(i);
+    const int shift = (8 - ((P.len2 * 4) % 8)) % 8;
+    csum <<= shift;
+    const int cbits = ((P.len2 * 4 + 7) / 8) * 8;  // checksum bytes as a big-endian integer
+    const int j = c - P.len1;
+    return (csum >> (cbits - 4 * (j + 1))) & 15u;
+}
+
+// ===========================================================================
+// message phase: thread per signature
+// ===========================================================================
+template <class HF>
+__global__ void k_sign_msg(SetParams P, SignArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.count) return;
+    const uint8_t *sk = A.sk.row(i);
+    uint32_t skprf[W], opt[W], pk[2 * W], R[W];
+    HF::load(skprf, sk + N);
+    HF::load(pk, sk + 2 * N);
+    HF::load(pk + W, sk + 3 * N);
+    if (A.optrand) {
+        HF::load(opt, A.optrand + (uint64_t)i * N);
+    } else {
+#pragma unroll
+        for (int j = 0; j < W; j++) opt[j] = 0xadadadadu;
+    }
+    const uint8_t *m = A.msg.base + A.msg.off[i];
+    const uint64_t mlen = A.msg.len[i];
+    HF::prf_msg(R, skprf, opt, m, mlen);
+    uint8_t *sig = A.sig + (uint64_t)i * P.sig_bytes;
+    HF::store(sig, R);
+    uint8_t dg[64];
+    HF::h_msg(dg, P.dgst_bytes, R, pk, m, mlen);
+    SignWork w;
+    for (int j = 0; j < 48; j++) w.mhash[j] = j < P.fors_msg_bytes ? dg[j] : 0;
+    uint64_t t = 0;
+    for (int j = 0; j < P.tree_bytes; j++) t = (t << 8) | dg[P.fors_msg_bytes + j];
+    if (P.tree_bits < 64) t &= (~0ull) >> (64 - P.tree_bits);
+    uint32_t l = 0;
+    for (int j = 0; j < P.leaf_bytes; j++) l = (l << 8) | dg[P.fors_msg_bytes + P.tree_bytes + j];
+    l &= (~0u) >> (32 - P.leaf_bits);
+    w.tree = t;
+    w.idx_leaf = l;
+    w.flags = 0;
+    KeyRegs<N> key;
+    HF::key_init(key, sk, sk + 2 * N);
+#pragma unroll
+    for (int j = 0; j < 8; j++) w.mid[j] = key.mid[j];
+    A.work[i] = w;
+}
+
+// ===========================================================================
+// FORS sign: one warp per (signature, tree).  Lane l owns the contiguous
+// subtree of 2^(a-5) leaves starting at l*2^(a-5) and reduces it with a
+// shared-memory stack (treehash, utils.cu:189-241); the 32 subtree roots are
+// then reduced over 5 shuffle levels.  Auth-path nodes are written by
+// whichever lane holds them.
+// ===========================================================================
+template <class HF>
+__global__ void k_fors_sign(SetParams P, SignArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    extern __shared__ uint32_t smem[];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (uint64_t)A.count * P.k) return;
+    const uint32_t item = (uint32_t)(gw / P.k);
+    const int t = (int)(gw % P.k);
+    const SignWork wk = A.work[item];
+    const uint8_t *sk = A.sk.row(item);
+    KeyRegs<N> key;
+    key_from_work<HF>(key, sk, sk + 2 * N, wk);
+    const uint32_t idx = fors_index(wk.mhash, P.a, t);
+    const int sub = P.a - 5;                    // lane subtree height
+    const uint32_t per = 1u << sub;
+    const uint32_t off = (uint32_t)t << P.a;   // idx_offset
+    uint8_t *sigt = A.sig + (uint64_t)item * P.sig_bytes + N + (uint64_t)t * (P.a + 1) * N;
+
+    Adrs ad;  // FORS tree address: layer 0, tree, key pair idx_leaf, type FORSTREE
+    adrs_zero(ad);
+    adrs_tree(ad, wk.tree);
+    adrs_keypair(ad, wk.idx_leaf);
+    adrs_type(ad, ADDR_FORSTREE);
+
+    // per-lane stack: (sub+1) entries of W words, plus heights
+    uint32_t *stk = smem + threadIdx.x * (P.a - 4) * W;   // sub+1 entries
+    int heights[16];
+    int sp = 0;
+    uint32_t v[W];
+    for (uint32_t jj = 0; jj < per; jj++) {
+        const uint32_t j = lane * per + jj;
+        adrs_height(ad, 0);
+        adrs_index(ad, off + j);
+        uint32_t skv[W];
+        HF::PRF(skv, ad, key);
+        if (j == idx) HF::store(sigt, skv);
+        HF::F(v, skv, ad, key);
+        if ((idx ^ 1u) == j) HF::store(sigt + N, v);
+        int hgt = 0;
+        // merge equal-height nodes on the stack
+        while (sp > 0 && heights[sp - 1] == hgt) {
+            uint32_t l[W];
+#pragma unroll
+            for (int q = 0; q < W; q++) l[q] = stk[(sp - 1) * W + q];
+            const uint32_t tidx = j >> (hgt + 1);
+            adrs_height(ad, hgt + 1);
+            adrs_index(ad, tidx + (off >> (hgt + 1)));
+            HF::H(v, l, v, ad, key);
+            sp--;
+            hgt++;
+            if (((idx >> hgt) ^ 1u) == tidx) HF::store(sigt + N + (uint64_t)hgt * N, v);
+        }
+#pragma unroll
+        for (int q = 0; q < W; q++) stk[sp * W + q] = v[q];
+        heights[sp] = hgt;
+        sp++;
+    }
+    // v = this lane's subtree root at height `sub`, index lane
+    for (int s = 0; s < 5; s++) {
+        const int hgt = sub + s;
+        const uint32_t q = lane >> s;
+        const bool holder = (lane & ((1u << s) - 1)) == 0;
+        if (holder && ((idx >> hgt) ^ 1u) == q) HF::store(sigt + N + (uint64_t)hgt * N, v);
+        uint32_t r[W];
+#pragma unroll
+        for (int x = 0; x < W; x++) r[x] = __shfl_down_sync(0xffffffffu, v[x], 1u << s);
+        if ((lane & ((2u << s) - 1)) == 0) {
+            adrs_height(ad, hgt + 1);
+            adrs_index(ad, (q >> 1) + (off >> (hgt + 1)));
+            HF::H(v, v, r, ad, key);
+        }
+    }
+    if (lane == 0) HF::store(A.fors_roots + ((uint64_t)item * P.k + t) * N, v);
+}
+
+// ===========================================================================
+// XMSS leaves: one thread per (item, layer, leaf).  WOTS+ public key
+// (wots_gen_pk, wots.cu:176-185) streamed straight into T_len (the leaf,
+// sign.cu:87-102).  The signing leaf of each layer also records every chain
+// value so the WOTS signature (wots_sign, wots.cu:614-625) is a gather.
+// ===========================================================================
+struct LeafArgs {
+    uint32_t count;      // items
+    int layer0;          // first layer handled
+    int nlayers;         // layers per item
+    KeyRef sk;
+    const SignWork *work;  // null for key generation (tree 0, no signing leaf)
+    uint8_t *leaves;     // [item][layer-layer0][leaf] n bytes
+    uint8_t *chains;     // [item][layer][chain][16] n bytes, or null
+};
+
+template <class HF>
+__global__ void k_leaves(SetParams P, LeafArgs A) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    extern __shared__ uint32_t smem[];
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nleaf = 1u << P.hp;
+    if (gid >= (uint64_t)A.count * A.nlayers * nleaf) return;
+    const uint32_t item = (uint32_t)(gid / ((uint64_t)A.nlayers * nleaf));
+    const uint32_t rem = (uint32_t)(gid % ((uint64_t)A.nlayers * nleaf));
+    const int L = A.layer0 + (int)(rem >> P.hp);
+    const uint32_t j = rem & (nleaf - 1);
+    const uint8_t *sk = A.sk.row(item);
+    KeyRegs<N> key;
+    uint64_t tree_L = 0;
+    uint32_t idx_L = 0xffffffffu;
+    if (A.work) {
+        const SignWork wk = A.work[item];
+        key_from_work<HF>(key, sk, sk + 2 * N, wk);
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    } else {
+        HF::key_init(key, sk, sk + 2 * N);
+    }
+    const bool rec = A.chains && (j == idx_L);
+    uint8_t *chain = rec ? A.chains + (((uint64_t)item * P.d + L) * LEN) * 16 * N : nullptr;
+
+    Adrs wa, pa;
+    adrs_zero(wa);
+    adrs_layer(wa, L);
+    adrs_tree(wa, tree_L);
+    adrs_type(wa, ADDR_WOTS);
+    adrs_keypair(wa, j);
+    adrs_zero(pa);
+    adrs_copy_keypair(pa, wa);
+    adrs_type(pa, ADDR_WOTSPK);
+
+    typename HF::TStream ts;
+    HF::t_init(ts, smem + threadIdx.x * HF::kSmemWords, key, pa);
+    for (int c = 0; c < LEN; c++) {
+        uint32_t v[W];
+        adrs_chain(wa, c);
+        adrs_hash(wa, 0);
+        HF::PRF(v, wa, key);
+        if (rec) HF::store(chain + ((uint64_t)c * 16) * N, v);
+        for (int s = 0; s < 15; s++) {
+            adrs_hash(wa, s);
+            HF::F(v, v, wa, key);
+            if (rec) HF::store(chain + ((uint64_t)c * 16 + s + 1) * N, v);
+        }
+        HF::t_absorb(ts, v, key);
+    }
+    uint32_t leaf[W];
+    HF::t_final(leaf, ts);
+    HF::store(A.leaves + (((uint64_t)item * A.nlayers + (L - A.layer0)) * nleaf + j) * N, leaf);
+}
+
+// ===========================================================================
+// XMSS trees: one warp per (item, layer); the 2^hp leaves are reduced level
+// by level in shared memory (treehash node addresses, utils.cu:209-233).
+// Writes the auth path of the layer's signing leaf (or none for keygen) and
+// the root.
+// ===========================================================================
+struct TreeArgs {
+    uint32_t count;
+    int layer0, nlayers;
+    KeyRef sk;
+    const SignWork *work;   // null for key generation
+    const uint8_t *leaves;
+    uint8_t *roots;         // [item][layer-layer0] n bytes
+    uint8_t *sig;           // auth paths are written here when work != null
+};
+
+template <class HF>
+__global__ void k_trees(SetParams P, TreeArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    extern __shared__ uint32_t smem[];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t wib = threadIdx.x >> 5;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (uint64_t)A.count * A.nlayers) return;
+    const uint32_t item = (uint32_t)(gw / A.nlayers);
+    const int L = A.layer0 + (int)(gw % A.nlayers);
+    const uint32_t nleaf = 1u << P.hp;
+    uint32_t *nodes = smem + wib * (2 * nleaf * W);   // level l at offset (2*nleaf - 2*(nleaf>>l))
+    const uint8_t *sk = A.sk.row(item);
+    KeyRegs<N> key;
+    uint64_t tree_L = 0;
+    uint32_t idx_L = 0;
+    if (A.work) {
+        const SignWork wk = A.work[item];
+        key_from_work<HF>(key, sk, sk + 2 * N, wk);
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    } else {
+        HF::key_init(key, sk, sk + 2 * N);
+    }
+    const uint8_t *lv = A.leaves + (((uint64_t)item * A.nlayers + (L - A.layer0)) * nleaf) * N;
+    for (uint32_t q = lane; q < nleaf; q += 32) {
+        uint32_t v[W];
+        HF::load(v, lv + (uint64_t)q * N);
+#pragma unroll
+        for (int x = 0; x < W; x++) nodes[q * W + x] = v[x];
+    }
+    __syncwarp();
+    uint8_t *auth = nullptr;
+    if (A.work)
+        auth = A.sig + (uint64_t)item * P.sig_bytes + N + P.fors_bytes +
+               (uint64_t)L * (P.wots_bytes + P.hp * N) + P.wots_bytes;
+    Adrs ad;
+    adrs_zero(ad);
+    adrs_layer(ad, L);
+    adrs_tree(ad, tree_L);
+    adrs_type(ad, ADDR_HASHTREE);
+    uint32_t base = 0;  // offset (in nodes) of the current level
+    for (int h = 0; h < P.hp; h++) {
+        const uint32_t cnt = nleaf >> h;
+        if (auth && lane == 0) {
+            uint32_t v[W];
+            const uint32_t sib = (idx_L >> h) ^ 1u;
+#pragma unroll
+            for (int x = 0; x < W; x++) v[x] = nodes[(base + sib) * W + x];
+            HF::store(auth + (uint64_t)h * N, v);
+        }
+        const uint32_t nb = base + cnt;
+        for (uint32_t q = lane; q < cnt / 2; q += 32) {
+            uint32_t l[W], r[W], o[W];
+#pragma unroll
+            for (int x = 0; x < W; x++) {
+                l[x] = nodes[(base + 2 * q) * W + x];
+                r[x] = nodes[(base + 2 * q + 1) * W + x];
+            }
+            adrs_height(ad, h + 1);
+            adrs_index(ad, q);
+            HF::H(o, l, r, ad, key);
+#pragma unroll
+            for (int x = 0; x < W; x++) nodes[(nb + q) * W + x] = o[x];
+        }
+        __syncwarp();
+        base = nb;
+    }
+    if (lane == 0) {
+        uint32_t v[W];
+#pragma unroll
+        for (int x = 0; x < W; x++) v[x] = nodes[base * W + x];
+        HF::store(A.roots + ((uint64_t)item * A.nlayers + (L - A.layer0)) * N, v);
+    }
+}
+
+// ===========================================================================
+// sign finish: block per signature.  Thread 0 computes the FORS public key
+// T_k(roots) (fors.cu:141-142); then all threads gather each layer's WOTS
+// signature from the recorded chain values: layer 0 signs the FORS key,
+// layer L signs the root of layer L-1.
+// ===========================================================================
+template <class HF>
+__global__ void k_sign_finish(SetParams P, SignArgs A) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    extern __shared__ uint32_t smem[];
+    const uint32_t item = blockIdx.x;
+    if (item >= A.count) return;
+    uint32_t *forspk = smem;                   // W words
+    uint32_t *tbuf = smem + 8;                 // TStream scratch
+    const SignWork wk = A.work[item];
+    const uint8_t *sk = A.sk.row(item);
+    if (threadIdx.x == 0) {
+        KeyRegs<N> key;
+        key_from_work<HF>(key, sk, sk + 2 * N, wk);
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_tree(pa, wk.tree);
+        adrs_keypair(pa, wk.idx_leaf);
+        adrs_type(pa, ADDR_FORSPK);
+        typename HF::TStream ts;
+        HF::t_init(ts, tbuf, key, pa);
+        for (int t = 0; t < P.k; t++) {
+            uint32_t v[W];
+            HF::load(v, A.fors_roots + ((uint64_t)item * P.k + t) * N);
+            HF::t_absorb(ts, v, key);
+        }
+        uint32_t o[W];
+        HF::t_final(o, ts);
+#pragma unroll
+        for (int x = 0; x < W; x++) forspk[x] = o[x];
+        // the top layer root must equal the key's root; otherwise the key row
+        // is inconsistent (sk root does not match its seeds)
+        uint32_t top[W], skroot[W];
+        HF::load(top, A.roots + ((uint64_t)item * P.d + (P.d - 1)) * N);
+        HF::load(skroot, sk + 3 * N);
+        bool ok = true;
+#pragma unroll
+        for (int x = 0; x < W; x++) ok &= top[x] == skroot[x];
+        if (A.status) A.status[item] = ok ? 0 : -2;
+    }
+    __syncthreads();
+    uint8_t *sig = A.sig + (uint64_t)item * P.sig_bytes;
+    for (int e = threadIdx.x; e < P.d * LEN; e += blockDim.x) {
+        const int L = e / LEN, c = e % LEN;
+        uint32_t msg[W];
+        if (L == 0) {
+#pragma unroll
+            for (int x = 0; x < W; x++) msg[x] = forspk[x];
+        } else {
+            HF::load(msg, A.roots + ((uint64_t)item * P.d + (L - 1)) * N);
+        }
+        const uint32_t ln = chain_len<HF>(P, msg, c);
+        const uint8_t *src = A.chains + ((((uint64_t)item * P.d + L) * LEN + c) * 16 + ln) * N;
+        uint32_t v[W];
+        load_bytes_le<N>(v, src);
+        store_bytes_le<N>(sig + N + P.fors_bytes + (uint64_t)L * (P.wots_bytes + P.hp * N) + (uint64_t)c * N, v);
+    }
+}
+
+// ===========================================================================
+// verify
+// ===========================================================================
+struct VerifyArgs {
+    uint32_t count;
+    KeyRef pk;
+    MsgRef msg;
+    const uint8_t *sig;         // count x sig_bytes (row stride sig_stride)
+    uint64_t sig_stride;
+    const uint64_t *siglen;     // per item, or null = sig_bytes
+    SignWork *work;
+    uint8_t *fors_roots;        // count x k x n
+    int32_t *verdict;           // 0 accept, -1 reject (crypto_sign_verify)
+};
+
+template <class HF>
+__global__ void k_verify_msg(SetParams P, VerifyArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.count) return;
+    SignWork w;
+    w.flags = 0;
+    if (A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes) {
+        w.flags = 1;  // wrong length: reject without hashing (sign.cu:3063-3065)
+        w.tree = 0;
+        w.idx_leaf = 0;
+        for (int j = 0; j < 48; j++) w.mhash[j] = 0;
+        A.work[i] = w;
+        return;
+    }
+    const uint8_t *pkb = A.pk.row(i);
+    const uint8_t *sig = A.sig + (uint64_t)i * A.sig_stride;
+    uint32_t R[W], pk[2 * W];
+    HF::load(R, sig);
+    HF::load(pk, pkb);
+    HF::load(pk + W, pkb + N);
+    uint8_t dg[64];
+    HF::h_msg(dg, P.dgst_bytes, R, pk, A.msg.base + A.msg.off[i], A.msg.len[i]);
+    for (int j = 0; j < 48; j++) w.mhash[j] = j < P.fors_msg_bytes ? dg[j] : 0;
+    uint64_t t = 0;
+    for (int j = 0; j < P.tree_bytes; j++) t = (t << 8) | dg[P.fors_msg_bytes + j];
+    if (P.tree_bits < 64) t &= (~0ull) >> (64 - P.tree_bits);
+    uint32_t l = 0;
+    for (int j = 0; j < P.leaf_bytes; j++) l = (l << 8) | dg[P.fors_msg_bytes + P.tree_bytes + j];
+    l &= (~0u) >> (32 - P.leaf_bits);
+    w.tree = t;
+    w.idx_leaf = l;
+    KeyRegs<N> key;
+    HF::key_init(key, pkb, pkb);
+#pragma unroll
+    for (int j = 0; j < 8; j++) w.mid[j] = key.mid[j];
+    A.work[i] = w;
+}
+
+// root from a leaf and its auth path (compute_root, utils.cu:94-135)
+template <class HF>
+SPX_DEV void compute_root(uint32_t root[HF::W], const uint32_t leaf[HF::W], uint32_t leaf_idx, uint32_t idx_offset,
+                          const uint8_t *auth, int height, Adrs &ad, const KeyRegs<4 * HF::W> &key) {
+    constexpr int W = HF::W, N = 4 * W;
+    uint32_t cur[W];
+#pragma unroll
+    for (int x = 0; x < W; x++) cur[x] = leaf[x];
+    for (int i = 0; i < height; i++) {
+        uint32_t sib[W];
+        HF::load(sib, auth + (uint64_t)i * N);
+        const bool right = leaf_idx & 1u;
+        leaf_idx >>= 1;
+        idx_offset >>= 1;
+        adrs_height(ad, i + 1);
+        adrs_index(ad, leaf_idx + idx_offset);
+        if (right) HF::H(cur, sib, cur, ad, key);
+        else HF::H(cur, cur, sib, ad, key);
+    }
+#pragma unroll
+    for (int x = 0; x < W; x++) root[x] = cur[x];
+}
+
+// FORS roots from the signature: thread per (item, tree) (fors_pk_from_sig, fors.cu:596-631)
+template <class HF>
+__global__ void k_verify_fors(SetParams P, VerifyArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)A.count * P.k) return;
+    const uint32_t item = (uint32_t)(gid / P.k);
+    const int t = (int)(gid % P.k);
+    const SignWork wk = A.work[item];
+    if (wk.flags) return;
+    const uint8_t *pkb = A.pk.row(item);
+    KeyRegs<N> key;
+    key_from_work<HF>(key, pkb, pkb, wk);   // verify needs PUB_SEED only
+    const uint32_t idx = fors_index(wk.mhash, P.a, t);
+    const uint32_t off = (uint32_t)t << P.a;
+    const uint8_t *st = A.sig + (uint64_t)item * A.sig_stride + N + (uint64_t)t * (P.a + 1) * N;
+    Adrs ad;
+    adrs_zero(ad);
+    adrs_tree(ad, wk.tree);
+    adrs_keypair(ad, wk.idx_leaf);
+    adrs_type(ad, ADDR_FORSTREE);
+    adrs_height(ad, 0);
+    adrs_index(ad, idx + off);
+    uint32_t skv[W], leaf[W], root[W];
+    HF::load(skv, st);
+    HF::F(leaf, skv, ad, key);
+    compute_root<HF>(root, leaf, idx, off, st + N, P.a, ad, key);
+    HF::store(A.fors_roots + ((uint64_t)item * P.k + t) * N, root);
+}
+
+// hypertree: thread per item, serial over the d layers (the verifier's
+// data dependency: layer L signs the root of layer L-1)
+template <class HF>
+__global__ void k_verify_ht(SetParams P, VerifyArgs A) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    extern __shared__ uint32_t smem[];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.count) return;
+    const SignWork wk = A.work[i];
+    if (wk.flags) {
+        A.verdict[i] = -1;
+        return;
+    }
+    const uint8_t *pkb = A.pk.row(i);
+    KeyRegs<N> key;
+    key_from_work<HF>(key, pkb, pkb, wk);
+    uint32_t *tb = smem + threadIdx.x * HF::kSmemWords;
+    uint32_t root[W];
+    {
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_tree(pa, wk.tree);
+        adrs_keypair(pa, wk.idx_leaf);
+        adrs_type(pa, ADDR_FORSPK);
+        typename HF::TStream ts;
+        HF::t_init(ts, tb, key, pa);
+        for (int t = 0; t < P.k; t++) {
+            uint32_t v[W];
+            HF::load(v, A.fors_roots + ((uint64_t)i * P.k + t) * N);
+            HF::t_absorb(ts, v, key);
+        }
+        HF::t_final(root, ts);
+    }
+    const uint8_t *sig = A.sig + (uint64_t)i * A.sig_stride + N + P.fors_bytes;
+    for (int L = 0; L < P.d; L++) {
+        uint64_t tree_L;
+        uint32_t idx_L;
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+        Adrs wa, pa;
+        adrs_zero(wa);
+        adrs_layer(wa, L);
+        adrs_tree(wa, tree_L);
+        adrs_type(wa, ADDR_WOTS);
+        adrs_keypair(wa, idx_L);
+        adrs_zero(pa);
+        adrs_copy_keypair(pa, wa);
+        adrs_type(pa, ADDR_WOTSPK);
+        typename HF::TStream ts;
+        HF::t_init(ts, tb, key, pa);
+        for (int c = 0; c < LEN; c++) {
+            uint32_t v[W];
+            HF::load(v, sig + (uint64_t)c * N);
+            const uint32_t ln = chain_len<HF>(P, root, c);
+            adrs_chain(wa, c);
+            for (uint32_t s = ln; s < 15; s++) {
+                adrs_hash(wa, s);
+                HF::F(v, v, wa, key);
+            }
+            HF::t_absorb(ts, v, key);
+        }
+        uint32_t leaf[W];
+        HF::t_final(leaf, ts);
+        Adrs ta;
+        adrs_zero(ta);
+        adrs_layer(ta, L);
+        adrs_tree(ta, tree_L);
+        adrs_type(ta, ADDR_HASHTREE);
+        compute_root<HF>(root, leaf, idx_L, 0, sig + P.wots_bytes, P.hp, ta, key);
+        sig += P.wots_bytes + P.hp * N;
+    }
+    uint32_t pr[W];
+    HF::load(pr, pkb + N);
+    bool ok = true;
+#pragma unroll
+    for (int x = 0; x < W; x++) ok &= pr[x] == root[x];
+    A.verdict[i] = ok ? 0 : -1;
+}
+
+}  // namespace cuspx

@@ -1,0 +1,163 @@
+// spx_launch.cuh -- launch sequences for one hash family instantiation.
+//
+// Each translation unit (spx_family_*.cu) instantiates Family<HF> for its
+// (hash, n, robust) combinations and registers them in the dispatch table
+// that the host engine indexes by parameter set.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "spx_kernels.cuh"
+
+namespace cuspx {
+
+// launch mapping knobs (picked per parameter set by the autotuner)
+struct Tuning {
+    int leaf_block = 128;    // threads per block for k_leaves
+    int fors_block = 128;    // threads per block for k_fors_sign (multiple of 32)
+    int verify_block = 64;   // threads per block for k_verify_ht
+    int tree_warps = 4;      // warps per block for k_trees (upper bound)
+};
+
+struct KeygenArgs {
+    uint32_t count;
+    uint8_t *sk;       // count x 4n: SK_SEED || SK_PRF || PUB_SEED filled in, ROOT written
+    uint8_t *pk;       // count x 2n: written
+    uint8_t *leaves;   // count x 2^hp x n scratch
+    uint8_t *roots;    // count x n scratch
+};
+
+// Optional per-kernel timing: an event is recorded on the launch stream
+// after every kernel of a sequence (event 0 before the first).
+struct PhaseTimer {
+    static constexpr int kMax = 16;
+    cudaEvent_t ev[kMax + 1];
+    const char *names[kMax];
+    int n = 0;
+    void mark(const char *name, cudaStream_t s) {
+        if (n < kMax) {
+            names[n] = name;
+            cudaEventRecord(ev[n + 1], s);
+            n++;
+        }
+    }
+};
+#define CUSPX_MARK(pt, name, s) \
+    do {                        \
+        if (pt) (pt)->mark(name, s); \
+    } while (0)
+
+struct FamilyOps {
+    cudaError_t (*configure)();
+    void (*sign)(const SetParams &, const SignArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
+    void (*verify)(const SetParams &, const VerifyArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
+    void (*keygen)(const SetParams &, const KeygenArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
+    int smem_words;    // per-thread T_l stream scratch
+};
+
+// registry: [hash][n index 0..2][robust]
+extern FamilyOps g_family[2][3][2];
+
+inline unsigned ceil_div(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// finish key generation: sk.ROOT = pk.ROOT = top root, pk.PUB_SEED = sk.PUB_SEED
+template <int n>
+__global__ void k_keygen_finish(KeygenArgs A) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.count) return;
+    uint8_t *sk = A.sk + (uint64_t)i * 4 * n;
+    uint8_t *pk = A.pk + (uint64_t)i * 2 * n;
+    for (int j = 0; j < n; j++) {
+        const uint8_t r = A.roots[(uint64_t)i * n + j];
+        sk[3 * n + j] = r;
+        pk[n + j] = r;
+        pk[j] = sk[2 * n + j];
+    }
+}
+
+template <class HF>
+struct Family {
+    static constexpr int W = HF::W, N = 4 * W;
+
+    static cudaError_t configure() {
+        cudaError_t e;
+        const int big = 200 * 1024;
+        if ((e = cudaFuncSetAttribute(k_leaves<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_fors_sign<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_trees<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_verify_ht<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        return cudaSuccess;
+    }
+
+    static void trees(const SetParams &P, const TreeArgs &T, const Tuning &tu, cudaStream_t s) {
+        const uint64_t per_warp = 2ull * (1u << P.hp) * W * 4;
+        int wpb = (int)(48 * 1024 / per_warp);
+        if (wpb > tu.tree_warps) wpb = tu.tree_warps;
+        if (wpb < 1) wpb = 1;
+        const uint64_t warps = (uint64_t)T.count * T.nlayers;
+        k_trees<HF><<<ceil_div(warps, wpb), 32 * wpb, per_warp * wpb, s>>>(P, T);
+    }
+
+    static void sign(const SetParams &P, const SignArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
+        if (A.count == 0) return;
+        k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
+        CUSPX_MARK(pt, "k_sign_msg", s);
+        {
+            const int b = tu.fors_block;
+            const uint64_t threads = (uint64_t)A.count * P.k * 32;
+            k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - 4) * W * 4, s>>>(P, A);
+            CUSPX_MARK(pt, "k_fors_sign", s);
+        }
+        {
+            LeafArgs L{A.count, 0, P.d, A.sk, A.work, A.leaves, A.chains};
+            const int b = tu.leaf_block;
+            const uint64_t threads = (uint64_t)A.count * P.d * (1u << P.hp);
+            k_leaves<HF><<<ceil_div(threads, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, L);
+            CUSPX_MARK(pt, "k_leaves", s);
+        }
+        {
+            TreeArgs T{A.count, 0, P.d, A.sk, A.work, A.leaves, A.roots, A.sig};
+            trees(P, T, tu, s);
+            CUSPX_MARK(pt, "k_trees", s);
+        }
+        k_sign_finish<HF><<<A.count, 128, (8 + HF::kSmemWords) * 4, s>>>(P, A);
+        CUSPX_MARK(pt, "k_sign_finish", s);
+    }
+
+    static void verify(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
+        if (A.count == 0) return;
+        k_verify_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
+        CUSPX_MARK(pt, "k_verify_msg", s);
+        k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
+        CUSPX_MARK(pt, "k_verify_fors", s);
+        const int b = tu.verify_block;
+        k_verify_ht<HF><<<ceil_div(A.count, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, A);
+        CUSPX_MARK(pt, "k_verify_ht", s);
+    }
+
+    static void keygen(const SetParams &P, const KeygenArgs &K, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
+        if (K.count == 0) return;
+        KeyRef kr{K.sk, nullptr, (uint32_t)(4 * N)};
+        LeafArgs L{K.count, P.d - 1, 1, kr, nullptr, K.leaves, nullptr};
+        const int b = tu.leaf_block;
+        const uint64_t threads = (uint64_t)K.count * (1u << P.hp);
+        k_leaves<HF><<<ceil_div(threads, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, L);
+        CUSPX_MARK(pt, "k_leaves", s);
+        TreeArgs T{K.count, P.d - 1, 1, kr, nullptr, K.leaves, K.roots, nullptr};
+        trees(P, T, tu, s);
+        CUSPX_MARK(pt, "k_trees", s);
+        k_keygen_finish<N><<<ceil_div(K.count, 128), 128, 0, s>>>(K);
+        CUSPX_MARK(pt, "k_keygen_finish", s);
+    }
+
+    static FamilyOps ops() {
+        FamilyOps o;
+        o.configure = &configure;
+        o.sign = &sign;
+        o.verify = &verify;
+        o.keygen = &keygen;
+        o.smem_words = HF::kSmemWords;
+        return o;
+    }
+};
+
+}  // namespace cuspx

@@ -1,0 +1,125 @@
+/*
+ * cuspx.h -- batched SPHINCS+ engine for one GB300 (sm_103a): C ABI.
+ *
+ * This is the batched face that sits beside the NIST api.h drop-in
+ * (include/spx_api.h).  It replaces the reference's batched GPU launchers
+ * with per-item keys, messages of any length, per-item statuses and
+ * verdicts:
+ *   cuspx_keypair_batch  <- face_mdp_crypto_sign_keypair / face_mhp_crypto_sign_keypair
+ *                           (api.h:54-63, sign.cu:1214-1273, :1756-1807)
+ *   cuspx_sign_batch     <- face_mdp_crypto_sign / face_mhp_crypto_sign_scheme2
+ *                           (api.h:117-131, sign.cu:5098-5195, :5920-5963)
+ *   cuspx_verify_batch   <- face_mdp_crypto_sign_open / face_mhp_crypto_sign_open
+ *                           (api.h:150-177, sign.cu:6856-6955, :7557-7598)
+ * The reference faces fix mlen = 32, use identical keys and return one
+ * aggregate verdict; these take per-item keys, lengths and verdicts.
+ *
+ * Every call returns 0 (CUSPX_OK) or a negative CUSPX_E* code and never
+ * aborts; cuspx_error() describes the last failure of a context.
+ * Buffers are caller-owned.  Byte layouts follow the reference exactly:
+ *   sk  = SK_SEED || SK_PRF || PUB_SEED || ROOT   (4n bytes)
+ *   pk  = PUB_SEED || ROOT                         (2n bytes)
+ *   sig = R || FORS || d x (WOTS || AUTH)          (cuspx_set_sizes)
+ */
+#ifndef CUSPX_H
+#define CUSPX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUSPX_OK 0
+#define CUSPX_EINVAL (-1)     /* bad argument (size, set id, null pointer) */
+#define CUSPX_ECUDA (-2)      /* CUDA runtime error, see cuspx_error() */
+#define CUSPX_ENOMEM (-3)     /* device memory budget exceeded */
+#define CUSPX_EBUSY (-4)      /* queue full / would exceed admission budget */
+#define CUSPX_ETIMEDOUT (-5)  /* wait expired */
+
+enum { CUSPX_OP_KEYGEN = 0, CUSPX_OP_SIGN = 1, CUSPX_OP_VERIFY = 2 };
+
+typedef struct cuspx_ctx cuspx_ctx;
+typedef struct cuspx_batch cuspx_batch;
+
+/* ---- parameter sets (params.h:33-79 as a runtime table) --------------- */
+int cuspx_num_sets(void);
+/* "sha256-128f-simple", "shake256-256f-robust", ...; a bare "sha256-128f"
+ * names the simple set.  Returns the set id or CUSPX_EINVAL. */
+int cuspx_set_id(const char *name);
+const char *cuspx_set_name(int set);
+/* sizes in bytes (api.h:12-14, params.h:138-146); any pointer may be null */
+int cuspx_set_sizes(int set, size_t *pk_bytes, size_t *sk_bytes, size_t *sig_bytes, size_t *seed_bytes,
+                    int *n);
+
+/* ---- context ------------------------------------------------------------ */
+int cuspx_create(int device, cuspx_ctx **out);
+void cuspx_destroy(cuspx_ctx *ctx);
+const char *cuspx_error(const cuspx_ctx *ctx);
+/* replace the launch mapping of one set (autotuner output); values <= 0 keep defaults */
+int cuspx_set_tuning(cuspx_ctx *ctx, int set, int leaf_block, int fors_block, int verify_block, int tree_warps);
+int cuspx_get_tuning(cuspx_ctx *ctx, int set, int *leaf_block, int *fors_block, int *verify_block, int *tree_warps);
+
+/* ---- one-shot calls on host buffers (synchronous) ----------------------- */
+/* seeds: count x 3n; writes pks: count x 2n, sks: count x 4n
+ * (crypto_sign_seed_keypair, sign.cu:154-182, per item) */
+int cuspx_keypair_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *seeds, uint8_t *pks, uint8_t *sks);
+/* sks: count x 4n rows; message i is msgs[msg_off[i] .. +msg_len[i]);
+ * optrand: count x n or NULL for the reference's fixed 0xAD bytes
+ * (sign.cu:1950-1954); sigs: count x sig_bytes; status[i] = 0 on success,
+ * -2 if the key's ROOT does not match its seeds (may be NULL). */
+int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, const uint8_t *msgs,
+                     const uint64_t *msg_off, const uint64_t *msg_len, const uint8_t *optrand, uint8_t *sigs,
+                     int32_t *status);
+/* pks: count x 2n rows; sigs: count rows of sig_bytes; siglens: per item
+ * (NULL = sig_bytes).  verdicts[i] = 0 accept, -1 reject
+ * (crypto_sign_verify, sign.cu:3048-3121). */
+int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks, const uint8_t *msgs,
+                       const uint64_t *msg_off, const uint64_t *msg_len, const uint8_t *sigs,
+                       const uint64_t *siglens, int32_t *verdicts);
+
+/* ---- reusable device-resident batches ----------------------------------
+ * A batch owns device buffers for up to `capacity` items of one op and set,
+ * its own CUDA stream and a CUDA graph of its launch sequence (captured on
+ * the first run of each item count).  upload/run/download are asynchronous
+ * on that stream; download and sync wait.  Message offsets passed to upload
+ * must be multiples of 16. */
+int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t msg_capacity, size_t key_capacity,
+                       cuspx_batch **out);
+void cuspx_batch_destroy(cuspx_batch *b);
+/* keys: nkeys rows (sk for keygen/sign -- keygen rows carry the seed in
+ * their first 3n bytes -- pk for verify); key_index: per item row, or NULL
+ * for row i.  aux: sign -> optrand (count x n) or NULL; verify -> sigs
+ * (count x sig_bytes); siglens: verify only, may be NULL. */
+int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t nkeys, const uint32_t *key_index,
+                       const uint8_t *msgs, size_t msg_bytes, const uint64_t *msg_off, const uint64_t *msg_len,
+                       const uint8_t *aux, const uint64_t *siglens);
+int cuspx_batch_run(cuspx_batch *b);
+/* sign -> out = sigs; verify -> out unused (verdicts in status);
+ * keygen -> out = sk rows, out2 = pk rows */
+int cuspx_batch_download(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status);
+int cuspx_batch_sync(cuspx_batch *b);
+/* device time of the last run, from CUDA events recorded on the batch stream */
+int cuspx_batch_last_ms(cuspx_batch *b, float *ms);
+/* the batch's cudaStream_t */
+void *cuspx_batch_stream(cuspx_batch *b);
+/* device pointers of the batch buffers (for device-resident callers) */
+int cuspx_batch_device_ptrs(cuspx_batch *b, void **keys, void **msgs, void **msg_off, void **msg_len, void **aux,
+                            void **out, void **status);
+/* per-kernel timing: when enabled, run() launches without the graph and
+ * records an event pair around every kernel; cuspx_batch_kernel_ms returns
+ * the names and accumulated milliseconds (count entries). */
+int cuspx_batch_profile(cuspx_batch *b, int enable);
+int cuspx_batch_kernel_ms(cuspx_batch *b, int idx, const char **name, double *ms, long *launches);
+
+/* ---- calibration --------------------------------------------------------
+ * Measured integer-ALU peak of this GPU for the hash cores' instruction mix
+ * (funnel-shift rotate, 3-input logic, 3-input add) on all SMs at full
+ * occupancy: the roofline denominator for the hash kernels. */
+int cuspx_int_peak(int device, int iters, double *ops_per_s, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

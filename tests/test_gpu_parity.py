@@ -1,0 +1,132 @@
+"""GPU parity: the engine (through the C ABI) against the reference's own
+outputs (tests/golden, written by tests/golden/make_golden.py from the
+reference CPU code) and against the C restatement in oracle/ for cases the
+fixtures do not hold (distinct keys, robust sets, long messages).
+
+Everything here is integer/byte work, so the bar is byte equality.
+"""
+import hashlib
+import os
+import random
+
+import pytest
+
+from conftest import GOLDEN, load_golden
+
+pytestmark = pytest.mark.gpu
+
+SIMPLE_SETS = ["sha256-128f", "sha256-128s", "sha256-192f", "sha256-192s", "sha256-256f", "sha256-256s",
+               "shake256-128f", "shake256-128s", "shake256-192f", "shake256-192s", "shake256-256f", "shake256-256s"]
+
+
+def _oracle(name):
+    import spx_oracle
+    return spx_oracle.Oracle(name)
+
+
+@pytest.mark.parametrize("setname", SIMPLE_SETS)
+def test_keypair_matches_reference(engine, setname):
+    g = load_golden(setname)
+    sid = engine.set_id(setname)
+    seeds = [bytes.fromhex(g["seed"]), bytes(range(g["seed_bytes"]))]
+    pks, sks = engine.keypair_batch(sid, seeds)
+    assert pks[0].hex() == g["pk"] and sks[0].hex() == g["sk"]
+    # crypto_sign_keypair under the shipped DEBUG_MODE uses seed 0..3n-1
+    assert pks[1].hex() == g["debug_keypair"]["pk"] and sks[1].hex() == g["debug_keypair"]["sk"]
+
+
+@pytest.mark.parametrize("setname", SIMPLE_SETS)
+def test_sign_matches_reference(engine, setname):
+    g = load_golden(setname)
+    sid = engine.set_id(setname)
+    sk = bytes.fromhex(g["sk"])
+    msgs = [bytes.fromhex(c["msg"]) for c in g["cases"]]
+    sigs, status = engine.sign_batch(sid, [sk] * len(msgs), msgs)
+    assert list(status) == [0] * len(msgs)
+    for c, sig in zip(g["cases"], sigs):
+        assert len(sig) == g["sig_bytes"]
+        assert sig[:64].hex() == c["sig_head"], "mlen=%d" % c["mlen"]
+        assert hashlib.sha256(sig).hexdigest() == c["sig_sha256"], "mlen=%d" % c["mlen"]
+        if "sig_file" in c:
+            with open(os.path.join(GOLDEN, c["sig_file"]), "rb") as f:
+                assert sig == f.read()
+
+
+@pytest.mark.parametrize("setname", SIMPLE_SETS)
+def test_verify_matches_reference(engine, setname):
+    """Good signatures accept; every corruption the reference rejected is rejected."""
+    g = load_golden(setname)
+    sid = engine.set_id(setname)
+    sk, pk = bytes.fromhex(g["sk"]), bytes.fromhex(g["pk"])
+    msgs = [bytes.fromhex(c["msg"]) for c in g["cases"]]
+    sigs, _ = engine.sign_batch(sid, [sk] * len(msgs), msgs)
+    vs_pk, vs_m, vs_sig, vs_len, want = [], [], [], [], []
+    for c, m, sig in zip(g["cases"], msgs, sigs):
+        vs_pk.append(pk); vs_m.append(m); vs_sig.append(sig); vs_len.append(len(sig)); want.append(c["verify"])
+        for fl in c["corrupt"]:
+            bad = bytearray(sig)
+            bad[fl["pos"]] ^= fl["xor"]
+            vs_pk.append(pk); vs_m.append(m); vs_sig.append(bytes(bad)); vs_len.append(len(sig))
+            want.append(fl["verify"])
+        if "msgflip_verify" in c:
+            bm = bytearray(m)
+            bm[len(m) // 2] ^= 0x10
+            vs_pk.append(pk); vs_m.append(bytes(bm)); vs_sig.append(sig); vs_len.append(len(sig))
+            want.append(c["msgflip_verify"])
+        vs_pk.append(pk); vs_m.append(m); vs_sig.append(sig); vs_len.append(len(sig) - 1)
+        want.append(c["shortsig_verify"])
+    got = engine.verify_batch(sid, vs_pk, vs_m, vs_sig, siglens=vs_len)
+    assert list(got) == want
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-128f-simple", "sha256-192f-robust",
+                                     "sha256-128f-robust", "shake256-256f-robust", "shake256-128f-robust"])
+def test_distinct_keys_uneven_lengths_vs_oracle(engine, setname):
+    """A batch with distinct keys and uneven lengths equals the oracle item by item."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(1234)
+    n = o.p.n
+    seeds = [bytes(rng.randrange(256) for _ in range(3 * n)) for _ in range(4)]
+    pks, sks = engine.keypair_batch(sid, seeds)
+    for s, pk, sk in zip(seeds, pks, sks):
+        opk, osk = o.seed_keypair(s)
+        assert (pk, sk) == (opk, osk)
+    lens = [0, 1, 17, 55, 56, 64, 100, 333]
+    msgs = [bytes(rng.randrange(256) for _ in range(L)) for L in lens]
+    key_of = [i % 4 for i in range(len(msgs))]
+    optrand = [bytes(rng.randrange(256) for _ in range(n)) for _ in msgs]
+    sigs, st = engine.sign_batch(sid, [sks[k] for k in key_of], msgs, optrand=optrand)
+    assert list(st) == [0] * len(msgs)
+    for m, k, opt, sig in zip(msgs, key_of, optrand, sigs):
+        assert sig == o.sign(m, sks[k], opt), "mlen=%d" % len(m)
+    v = engine.verify_batch(sid, [pks[k] for k in key_of], msgs, sigs)
+    assert list(v) == [0] * len(msgs)
+    # wrong key rejects
+    v = engine.verify_batch(sid, [pks[(k + 1) % 4] for k in key_of], msgs, sigs)
+    assert list(v) == [-1] * len(msgs)
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-128f-simple"])
+def test_long_message_vs_oracle(engine, setname):
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(7)
+    seed = bytes(rng.randrange(256) for _ in range(3 * o.p.n))
+    pk, sk = o.seed_keypair(seed)
+    msgs = [bytes(rng.randrange(256) for _ in range(L)) for L in (65536, 4097, 1000)]
+    sigs, _ = engine.sign_batch(sid, [sk] * 3, msgs)
+    for m, s in zip(msgs, sigs):
+        assert s == o.sign(m, sk)
+    assert list(engine.verify_batch(sid, [pk] * 3, msgs, sigs)) == [0, 0, 0]
+
+
+def test_sign_status_flags_bad_key(engine):
+    """A secret key whose ROOT does not match its seeds is reported per item."""
+    sid = engine.set_id("sha256-128f-simple")
+    g = load_golden("sha256-128f")
+    sk = bytearray.fromhex(g["sk"])
+    bad = bytearray(sk)
+    bad[-1] ^= 1
+    _, st = engine.sign_batch(sid, [bytes(sk), bytes(bad)], [b"abc", b"abc"])
+    assert list(st) == [0, -2]

@@ -1,0 +1,431 @@
+"""Benchmark: batched SPHINCS+-SHA-256-128f-simple signing on one GB300.
+
+Workload (the batched configuration the headline metric is quoted on): one
+keypair, 4096 messages of 64 uniform random bytes, all signed in one
+graph-launched batch, then all 4096 verified in one batch; the signatures of a
+seeded 64-message subset are byte-compared with the CPU oracle.
+
+A step is one sign batch of 4096 messages.  `value` is signs/s with inputs
+already resident in HBM (device time from CUDA events on the batch stream);
+`e2e` is the same through the C ABI with pinned host buffers, the
+host->device copy of messages/key and the device->host copy of all
+signatures inside every timed step.  Verify throughput, the plain
+one-signature-per-call path and the roofline of the dominant kernel
+(k_leaves) ride along on the same JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N>1 runs under torchrun as independent replicas (the path shards by request,
+no collective): every rank signs its own 4096 messages, value sums the ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SET = "sha256-128f-simple"
+BATCH = 4096
+MLEN = 64
+SUBSET = 64
+METRIC = "sign/s & verify/s, SHA2-128f, 1 GB300: batched+served vs plain; p50/p99 latency"
+# SHA-256 compressions per XMSS leaf for 128f (35 chains x (PRF + 15 F) + 10 T_len blocks)
+LEAF_CMP = {16: 35 * 16 + 10, 24: 51 * 16 + 20, 32: 67 * 16 + 36}
+OPS_PER_CMP = 1384   # INT ops of one SHA-256 compression (64 rounds x 14 + 48 x 10 + 8)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = []
+        mx = 0.0
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for i, nm in enumerate(names):
+                    if r[5 + i].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(rank):
+    import numpy as np
+    import cuspx_gb300 as c
+    rng = np.random.default_rng(20260 + rank)
+    seed = rng.bytes(48)
+    msgs = rng.integers(0, 256, size=(BATCH, MLEN), dtype=np.uint8)
+    return seed, msgs
+
+
+def cpu_baseline_port(seconds):
+    """The C restatement of the reference CPU path, all host cores, bounded."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+    o = spx_oracle.Oracle(SET)
+    threads = os.cpu_count() or 1
+    done, secs = o.throughput(0, threads, MLEN, seconds)
+    vdone, vsecs = o.throughput(1, threads, MLEN, max(1.0, seconds / 4))
+    return {"value": done / secs if secs else 0.0, "unit": "sign/s", "cores": threads, "kind": "port",
+            "sample": "%d signatures of %d-B messages (%s) on %d threads in %.1f s, each worker its own key" %
+                      (done, MLEN, SET, threads, secs),
+            "verify_per_s": vdone / vsecs if vsecs else 0.0}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    per_step = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        sample_s = 2.0
+        info = cpu_baseline_port(sample_s)
+        if i >= args.warmup:
+            per_step.append(info["value"])
+    value = statistics.median(per_step)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sign/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * BATCH / value if value else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded uniform random 64-B messages)",
+            "config": {"workload": "batched SHA-256-128f-simple sign, 4096 x 64-B messages, one key",
+                       "set": SET, "batch": BATCH, "mlen": MLEN,
+                       "reference_code": "C restatement of the reference CPU path (oracle/spx_oracle.c); the "
+                                         "reference's own sources are absent on the GPU host"},
+            "cpu_baseline": {"value": value, "unit": "sign/s", "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": value, "unit": "sign/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0,
+                    help="run one sign and one verify batch of this many messages (for ncu) and exit")
+    ap.add_argument("--profile-set", default=SET)
+    args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args.profile_case, args.profile_set)
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import cuspx_gb300 as c
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    eng = c.Engine(local)
+    sid = c.set_id(SET)
+    z = c.set_sizes(sid)
+    peak_ops, _ = c.int_peak(local, 8192)
+
+    seed, msgs = make_inputs(rank)
+    pks, sks = eng.keypair_batch(sid, [seed])
+    pk, sk = pks[0], sks[0]
+    slab = np.ascontiguousarray(msgs.reshape(-1))
+    offs = np.arange(BATCH, dtype=np.uint64) * MLEN
+    lens = np.full(BATCH, MLEN, dtype=np.uint64)
+    kidx = np.zeros(BATCH, dtype=np.uint32)
+    skb = np.frombuffer(sk, dtype=np.uint8).copy()
+    pkb = np.frombuffer(pk, dtype=np.uint8).copy()
+
+    # pinned host buffers for the end-to-end path
+    def pinned(nbytes):
+        return torch.empty(max(1, nbytes), dtype=torch.uint8, pin_memory=True).numpy()
+    h_msgs = pinned(slab.nbytes); h_msgs[:] = slab
+    h_offs = pinned(offs.nbytes).view(np.uint64); h_offs[:] = offs
+    h_lens = pinned(lens.nbytes).view(np.uint64); h_lens[:] = lens
+    h_kidx = pinned(kidx.nbytes).view(np.uint32); h_kidx[:] = kidx
+    h_sk = pinned(skb.nbytes); h_sk[:] = skb
+    h_sigs = pinned(BATCH * z["sig"])
+    h_status = pinned(BATCH * 4).view(np.int32)
+
+    sb = eng.batch(c.OP_SIGN, sid, BATCH, slab.nbytes, 1)
+    vb = eng.batch(c.OP_VERIFY, sid, BATCH, slab.nbytes, 1)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
+
+    # ---- correctness gate: seeded 64-message subset against the oracle ----
+    sb.upload(BATCH, h_sk, 1, h_kidx, h_msgs, slab.nbytes, h_offs, h_lens)
+    sb.run()
+    sb.download(h_sigs, None, h_status)
+    assert (h_status == 0).all(), "sign status"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+    o = spx_oracle.Oracle(SET)
+    rs = np.random.default_rng(64)
+    subset = sorted(rs.choice(BATCH, SUBSET, replace=False).tolist())
+    for i in subset:
+        ref = o.sign(bytes(msgs[i]), sk)
+        got = bytes(h_sigs[i * z["sig"]:(i + 1) * z["sig"]])
+        assert got == ref, "signature %d differs from the CPU oracle" % i
+    vb.upload(BATCH, pkb, 1, h_kidx, h_msgs, slab.nbytes, h_offs, h_lens, h_sigs)
+    vb.run()
+    vv = np.zeros(BATCH, dtype=np.int32)
+    vb.download(None, None, vv)
+    assert (vv == 0).all(), "verify rejected a valid signature"
+
+    # ---- device-resident timing (value) ----
+    for _ in range(args.warmup):
+        sb.run(); vb.run()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    sign_ms, verify_ms = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sb.run(); sb.sync(); sign_ms.append(sb.last_ms())
+        flush.zero_()
+        torch.cuda.synchronize()
+        vb.run(); vb.sync(); verify_ms.append(vb.last_ms())
+    barrier()
+    wall = time.perf_counter() - t0
+    ck = clocks.stop()
+    sign_total = sum(sign_ms)
+    verify_total = sum(verify_ms)
+    if world > 1:
+        t = torch.tensor([sign_total, verify_total], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sign_total, verify_total = t.tolist()
+    value = world * BATCH * args.steps / (sign_total / 1e3)
+    verify_value = world * BATCH * args.steps / (verify_total / 1e3)
+
+    # ---- per-kernel times (events around each kernel, same stream) ----
+    sb.profile(True)
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sb.run(); sb.sync()
+    kern = sb.kernel_ms()
+    sb.profile(False)
+    vb.profile(True)
+    vb.run(); vb.sync()
+    vkern = vb.kernel_ms()
+    vb.profile(False)
+    tot = sum(m for _, m, _ in kern)
+    leaves = [(m / n) for name, m, n in kern if name == "k_leaves"][0]
+    P = dict(n=16, d=22, hp=3)
+    leaf_ops = BATCH * P["d"] * (1 << P["hp"]) * LEAF_CMP[P["n"]] * OPS_PER_CMP
+    achieved = leaf_ops / (leaves * 1e-3) / 1e12
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "k_leaves_sha256-128f_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tj = json.load(f)
+        traffic = tj.get("dram_bytes_per_launch_scaled_to_4096")
+
+    # ---- end-to-end through the C ABI with host buffers ----
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        sb.upload(BATCH, h_sk, 1, h_kidx, h_msgs, slab.nbytes, h_offs, h_lens)
+        sb.run()
+        sb.download(h_sigs, None, h_status)
+        s1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_ms.append((s1 - s0) * 1e3)
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = t.item()
+    e2e_value = world * BATCH * args.steps / (e2e_total / 1e3)
+    h2d = slab.nbytes + skb.nbytes + offs.nbytes + lens.nbytes + kidx.nbytes
+    d2h = BATCH * z["sig"] + BATCH * 4
+
+    # ---- plain one-signature-per-call path (NIST api.h drop-in) ----
+    plain = None
+    if rank == 0:
+        plain = plain_path(c)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_port(args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "sign/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sign_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded uniform random 64-B messages; one seeded keypair)",
+            "config": {"workload": "batched SHA-256-128f-simple: 4096 x 64-B messages signed in one "
+                                   "graph-launched batch, then verified in one batch",
+                       "set": SET, "batch": BATCH, "mlen": MLEN, "parallelism": "replicas" if world > 1 else "1gpu",
+                       "l2": "256 MiB buffer written between timed steps (L2 is 129 MB)",
+                       "subset_check": "%d seeded signatures byte-identical to the CPU oracle" % SUBSET},
+            "verify": {"value": verify_value, "unit": "verify/s", "ms_per_batch": verify_total / args.steps},
+            "e2e": {"value": e2e_value, "unit": "sign/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_total / args.steps},
+            "gpu_launches": (5 + 3) * args.steps,
+            "kernels_ms": {name: round(m / n, 4) for name, m, n in kern},
+            "verify_kernels_ms": {name: round(m / n, 4) for name, m, n in vkern},
+            "roofline": {"bound": "int_alu", "kernel": "k_leaves", "achieved": achieved,
+                         "peak": peak_ops / 1e12, "unit": "Tops/s", "frac": achieved / (peak_ops / 1e12),
+                         "traffic": traffic,
+                         "work": "%d compressions x %d INT ops per launch" %
+                                 (BATCH * 176 * LEAF_CMP[16], OPS_PER_CMP),
+                         "peak_source": "measured in this run: SHF/LOP3/IADD3 mix on all SMs (cuspx_int_peak)",
+                         "share_of_step": leaves / (tot / 3)},
+            "clocks": ck,
+            "wall_s_timed": wall,
+        }
+        if plain:
+            line["plain"] = plain
+            line["batched_vs_plain"] = value / plain["sign_per_s"] if plain["sign_per_s"] else None
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    sb.close(); vb.close(); eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def profile_case(count, setname):
+    """One sign batch and one verify batch of `count` 64-B messages, kernels
+    launched directly on the batch stream (no graph): the small case that
+    ncu captures."""
+    import numpy as np
+    import cuspx_gb300 as c
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+    eng = c.Engine(0)
+    sid = c.set_id(setname)
+    z = c.set_sizes(sid)
+    rng = np.random.default_rng(11)
+    # key from the CPU oracle, so the first GPU launches are the signing ones
+    pk0, sk0 = spx_oracle.Oracle(setname).seed_keypair(rng.bytes(z["seed"]))
+    pks, sks = [pk0], [sk0]
+    msgs = [rng.bytes(MLEN) for _ in range(count)]
+    slab, offs, lens = c.pack_messages(msgs)
+    kidx = np.zeros(count, dtype=np.uint32)
+    sb = eng.batch(c.OP_SIGN, sid, count, len(slab), 1)
+    sb.profile(True)
+    sb.upload(count, sks[0], 1, kidx, slab, len(slab), offs, lens)
+    sb.run()
+    sigs = np.zeros(count * z["sig"], dtype=np.uint8)
+    st = np.zeros(count, dtype=np.int32)
+    sb.download(sigs, None, st)
+    vb = eng.batch(c.OP_VERIFY, sid, count, len(slab), 1)
+    vb.profile(True)
+    vb.upload(count, pks[0], 1, kidx, slab, len(slab), offs, lens, sigs)
+    vb.run()
+    vv = np.zeros(count, dtype=np.int32)
+    vb.download(None, None, vv)
+    ok = bool((st == 0).all() and (vv == 0).all())
+    print(json.dumps({"profile_case": setname, "count": count, "ok": ok,
+                      "sign_kernels_ms": {k: round(m, 3) for k, m, _ in sb.kernel_ms()},
+                      "verify_kernels_ms": {k: round(m, 3) for k, m, _ in vb.kernel_ms()}}))
+    sb.close(); vb.close(); eng.close()
+    return 0 if ok else 1
+
+
+def plain_path(c):
+    """configs[0]: one keypair, 16 messages of 32..1024 B, keypair/sign/verify
+    one call at a time through the NIST api.h drop-in library."""
+    import ctypes
+    import numpy as np
+    L = ctypes.CDLL(c.dropin_path(SET))
+    L.crypto_sign_signature.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p,
+                                        ctypes.c_size_t, ctypes.c_char_p]
+    L.crypto_sign_verify.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t,
+                                     ctypes.c_char_p]
+    L.crypto_sign_seed_keypair.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p]
+    rng = np.random.default_rng(7)
+    seed = rng.bytes(48)
+    pk = ctypes.create_string_buffer(32)
+    sk = ctypes.create_string_buffer(64)
+    t0 = time.perf_counter()
+    assert L.crypto_sign_seed_keypair(pk, sk, seed) == 0
+    kp_ms = (time.perf_counter() - t0) * 1e3
+    msgs = [rng.bytes(int(x)) for x in rng.integers(32, 1025, size=16)]
+    sig = ctypes.create_string_buffer(17088)
+    sl = ctypes.c_size_t()
+    L.crypto_sign_signature(sig, ctypes.byref(sl), msgs[0], len(msgs[0]), sk.raw)   # warm the path
+    s_lat, v_lat = [], []
+    for m in msgs:
+        t0 = time.perf_counter()
+        assert L.crypto_sign_signature(sig, ctypes.byref(sl), m, len(m), sk.raw) == 0
+        t1 = time.perf_counter()
+        assert L.crypto_sign_verify(sig.raw, sl.value, m, len(m), pk.raw) == 0
+        t2 = time.perf_counter()
+        s_lat.append((t1 - t0) * 1e3)
+        v_lat.append((t2 - t1) * 1e3)
+    return {"workload": "1 key, 16 messages 32..1024 B, one crypto_sign_signature / crypto_sign_verify "
+                        "call at a time through libspx_%s.so" % SET,
+            "sign_per_s": 1e3 * len(s_lat) / sum(s_lat), "verify_per_s": 1e3 * len(v_lat) / sum(v_lat),
+            "sign_ms_p50": statistics.median(s_lat), "verify_ms_p50": statistics.median(v_lat),
+            "keypair_ms": kp_ms}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -35,6 +35,15 @@ class CuspxError(RuntimeError):
     pass
 
 
+class Tuning(ctypes.Structure):
+    """cuspx_tuning: the launch mapping of one parameter set."""
+    _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
+                                            "chains_per_warp", "verify_mode")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -57,8 +66,8 @@ def lib():
     L.cuspx_destroy.restype = None
     L.cuspx_error.argtypes = [vp]
     L.cuspx_error.restype = c.c_char_p
-    L.cuspx_set_tuning.argtypes = [vp, c.c_int, c.c_int, c.c_int, c.c_int, c.c_int]
-    L.cuspx_get_tuning.argtypes = [vp, c.c_int] + [c.POINTER(c.c_int)] * 4
+    L.cuspx_set_tuning.argtypes = [vp, c.c_int, c.POINTER(Tuning)]
+    L.cuspx_get_tuning.argtypes = [vp, c.c_int, c.POINTER(Tuning)]
     L.cuspx_keypair_batch.argtypes = [vp, c.c_int, sz, vp, vp, vp]
     L.cuspx_sign_batch.argtypes = [vp, c.c_int, sz, vp, vp, vp, vp, vp, vp, vp]
     L.cuspx_verify_batch.argtypes = [vp, c.c_int, sz, vp, vp, vp, vp, vp, vp, vp]
@@ -177,14 +186,17 @@ class Engine:
     set_id = staticmethod(set_id)
     set_sizes = staticmethod(set_sizes)
 
-    def set_tuning(self, sid, leaf_block=0, fors_block=0, verify_block=0, tree_warps=0):
-        self._check(self.L.cuspx_set_tuning(self.h, sid, leaf_block, fors_block, verify_block, tree_warps),
-                    "set_tuning")
+    def set_tuning(self, sid, **kw):
+        """Change fields of a set's launch mapping (others keep their value)."""
+        t = Tuning(0, 0, 0, 0, 0, -1)
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")
 
     def get_tuning(self, sid):
-        v = [ctypes.c_int() for _ in range(4)]
-        self._check(self.L.cuspx_get_tuning(self.h, sid, *[ctypes.byref(x) for x in v]), "get_tuning")
-        return dict(leaf_block=v[0].value, fors_block=v[1].value, verify_block=v[2].value, tree_warps=v[3].value)
+        t = Tuning()
+        self._check(self.L.cuspx_get_tuning(self.h, sid, ctypes.byref(t)), "get_tuning")
+        return t.as_dict()
 
     def keypair_batch(self, sid, seeds):
         z = set_sizes(sid)

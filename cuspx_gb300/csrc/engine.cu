@@ -104,11 +104,13 @@ struct cuspx_batch {
     int32_t *status = nullptr;
     SignWork *work = nullptr;
     uint8_t *fors_roots = nullptr, *leaves = nullptr, *roots = nullptr, *chains = nullptr;
+    uint8_t *wpk = nullptr, *cur_root = nullptr;
     size_t count = 0;
     bool use_keyrow = false, use_aux = false, use_siglen = false;
     cudaGraphExec_t gexec = nullptr;
     size_t g_count = 0;
     bool g_keyrow = false, g_aux = false, g_siglen = false;
+    Tuning g_tune{};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     bool ran = false;
     bool profile = false;
@@ -188,35 +190,48 @@ void cuspx_destroy(cuspx_ctx *ctx) {
 
 const char *cuspx_error(const cuspx_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-int cuspx_set_tuning(cuspx_ctx *ctx, int set, int leaf_block, int fors_block, int verify_block, int tree_warps) {
-    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
-    Tuning &t = ctx->tune[set];
-    if (leaf_block > 0) {
-        if (leaf_block % 32 || leaf_block > 1024) return fail(ctx, CUSPX_EINVAL, "leaf_block must be a multiple of 32 <= 1024");
-        t.leaf_block = leaf_block;
+int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
+    if (!ctx || !in || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    Tuning t = ctx->tune[set];
+    auto blk = [&](int v, int &dst, const char *what) -> bool {
+        if (v <= 0) return true;
+        if (v % 32 || v > 1024) {
+            fail(ctx, CUSPX_EINVAL, std::string(what) + " must be a multiple of 32 <= 1024");
+            return false;
+        }
+        dst = v;
+        return true;
+    };
+    if (!blk(in->leaf_block, t.leaf_block, "leaf_block") || !blk(in->fors_block, t.fors_block, "fors_block") ||
+        !blk(in->verify_block, t.verify_block, "verify_block"))
+        return CUSPX_EINVAL;
+    if (in->tree_warps > 0) {
+        if (in->tree_warps > 32) return fail(ctx, CUSPX_EINVAL, "tree_warps must be <= 32");
+        t.tree_warps = in->tree_warps;
     }
-    if (fors_block > 0) {
-        if (fors_block % 32 || fors_block > 1024) return fail(ctx, CUSPX_EINVAL, "fors_block must be a multiple of 32 <= 1024");
-        t.fors_block = fors_block;
+    if (in->chains_per_warp > 0) {
+        if (in->chains_per_warp < 32 || in->chains_per_warp > 65536)
+            return fail(ctx, CUSPX_EINVAL, "chains_per_warp must be in [32, 65536]");
+        t.chains_per_warp = in->chains_per_warp;
     }
-    if (verify_block > 0) {
-        if (verify_block % 32 || verify_block > 1024) return fail(ctx, CUSPX_EINVAL, "verify_block must be a multiple of 32 <= 1024");
-        t.verify_block = verify_block;
+    if (in->verify_mode >= 0) {
+        if (in->verify_mode > 1) return fail(ctx, CUSPX_EINVAL, "verify_mode must be 0 or 1");
+        t.verify_mode = in->verify_mode;
     }
-    if (tree_warps > 0) {
-        if (tree_warps > 32) return fail(ctx, CUSPX_EINVAL, "tree_warps must be <= 32");
-        t.tree_warps = tree_warps;
-    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->tune[set] = t;   // batches re-capture their graph when the mapping changed
     return CUSPX_OK;
 }
 
-int cuspx_get_tuning(cuspx_ctx *ctx, int set, int *leaf_block, int *fors_block, int *verify_block, int *tree_warps) {
-    if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
+    if (!ctx || !out || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
     const Tuning &t = ctx->tune[set];
-    if (leaf_block) *leaf_block = t.leaf_block;
-    if (fors_block) *fors_block = t.fors_block;
-    if (verify_block) *verify_block = t.verify_block;
-    if (tree_warps) *tree_warps = t.tree_warps;
+    out->leaf_block = t.leaf_block;
+    out->fors_block = t.fors_block;
+    out->verify_block = t.verify_block;
+    out->tree_warps = t.tree_warps;
+    out->chains_per_warp = t.chains_per_warp;
+    out->verify_mode = t.verify_mode;
     return CUSPX_OK;
 }
 
@@ -291,6 +306,8 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
         } else {
             A((void **)&b->aux, cap * P.sig_bytes);
             A((void **)&b->siglen, cap * sizeof(uint64_t));
+            A((void **)&b->wpk, cap * P.len * n);
+            A((void **)&b->cur_root, cap * n);
         }
     }
     if (rc != CUSPX_OK) {
@@ -399,6 +416,8 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.work = b->work;
         A.fors_roots = b->fors_roots;
         A.verdict = b->status;
+        A.wpk = b->wpk;
+        A.cur_root = b->cur_root;
         ops.verify(P, A, tu, b->s, pt);
     } else {
         KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots};
@@ -439,8 +458,10 @@ int cuspx_batch_run(cuspx_batch *b) {
         b->ran = true;
         return CUSPX_OK;
     }
+    const Tuning &tu = ctx->tune[b->set];
     const bool stale = !b->gexec || b->g_count != b->count || b->g_keyrow != b->use_keyrow ||
-                       b->g_aux != b->use_aux || b->g_siglen != b->use_siglen;
+                       b->g_aux != b->use_aux || b->g_siglen != b->use_siglen ||
+                       memcmp(&b->g_tune, &tu, sizeof(Tuning)) != 0;
     if (stale) {
         if (b->gexec) {
             cudaGraphExecDestroy(b->gexec);
@@ -457,6 +478,7 @@ int cuspx_batch_run(cuspx_batch *b) {
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
         b->g_count = b->count;
+        b->g_tune = tu;
         b->g_keyrow = b->use_keyrow;
         b->g_aux = b->use_aux;
         b->g_siglen = b->use_siglen;

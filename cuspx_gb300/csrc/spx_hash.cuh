@@ -95,11 +95,13 @@ SPX_DEV void sha256_iv(uint32_t s[8]) {
     for (int i = 0; i < 8; i++) s[i] = sha256_iv_word(i);
 }
 
-// s <- compress(s, w); w is consumed (overwritten by the schedule).
-SPX_DEV void sha256_compress(uint32_t s[8], uint32_t w[16]) {
-    uint32_t a = s[0], b = s[1], c = s[2], d = s[3], e = s[4], f = s[5], g = s[6], h = s[7];
+// Rounds [R0, R1) of the compression on the working variables st = a..h;
+// w is the rolling 16-word schedule window (overwritten as it expands).
+template <int R0, int R1>
+SPX_DEV void sha256_rounds(uint32_t st[8], uint32_t w[16]) {
+    uint32_t a = st[0], b = st[1], c = st[2], d = st[3], e = st[4], f = st[5], g = st[6], h = st[7];
 #pragma unroll
-    for (int i = 0; i < 64; i++) {
+    for (int i = R0; i < R1; i++) {
         uint32_t wi;
         if (i < 16) {
             wi = w[i];
@@ -120,8 +122,17 @@ SPX_DEV void sha256_compress(uint32_t s[8], uint32_t w[16]) {
         b = a;
         a = t1 + t2;
     }
-    s[0] += a; s[1] += b; s[2] += c; s[3] += d;
-    s[4] += e; s[5] += f; s[6] += g; s[7] += h;
+    st[0] = a; st[1] = b; st[2] = c; st[3] = d; st[4] = e; st[5] = f; st[6] = g; st[7] = h;
+}
+
+// s <- compress(s, w); w is consumed (overwritten by the schedule).
+SPX_DEV void sha256_compress(uint32_t s[8], uint32_t w[16]) {
+    uint32_t t[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) t[i] = s[i];
+    sha256_rounds<0, 64>(t, w);
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[i] += t[i];
 }
 
 // ---------------------------------------------------------------------------

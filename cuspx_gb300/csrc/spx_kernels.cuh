@@ -312,9 +312,10 @@ __global__ void k_leaves(SetParams P, LeafArgs A) {
         adrs_hash(wa, 0);
         HF::PRF(v, wa, key);
         if (rec) HF::store(chain + ((uint64_t)c * 16) * N, v);
+        typename HF::FCtx fc;
+        HF::f_prepare(fc, wa, key);
         for (int s = 0; s < 15; s++) {
-            adrs_hash(wa, s);
-            HF::F(v, v, wa, key);
+            HF::f_step(v, v, fc, s, key);
             if (rec) HF::store(chain + ((uint64_t)c * 16 + s + 1) * N, v);
         }
         HF::t_absorb(ts, v, key);
@@ -492,6 +493,8 @@ struct VerifyArgs {
     SignWork *work;
     uint8_t *fors_roots;        // count x k x n
     int32_t *verdict;           // 0 accept, -1 reject (crypto_sign_verify)
+    uint8_t *wpk;               // count x len x n: WOTS public key of the current layer
+    uint8_t *cur_root;          // count x n: root of the layer below (FORS key for layer 0)
 };
 
 template <class HF>
@@ -640,10 +643,9 @@ __global__ void k_verify_ht(SetParams P, VerifyArgs A) {
             HF::load(v, sig + (uint64_t)c * N);
             const uint32_t ln = chain_len<HF>(P, root, c);
             adrs_chain(wa, c);
-            for (uint32_t s = ln; s < 15; s++) {
-                adrs_hash(wa, s);
-                HF::F(v, v, wa, key);
-            }
+            typename HF::FCtx fc;
+            HF::f_prepare(fc, wa, key);
+            for (uint32_t s = ln; s < 15; s++) HF::f_step(v, v, fc, s, key);
             HF::t_absorb(ts, v, key);
         }
         uint32_t leaf[W];
@@ -662,6 +664,164 @@ __global__ void k_verify_ht(SetParams P, VerifyArgs A) {
 #pragma unroll
     for (int x = 0; x < W; x++) ok &= pr[x] == root[x];
     A.verdict[i] = ok ? 0 : -1;
+}
+
+// ---------------------------------------------------------------------------
+// Layered verify.  The verifier is serial over the d layers (layer L signs
+// the root of layer L-1), so each layer is two flat kernels over the whole
+// batch instead of one thread walking all layers:
+//   k_verify_chains  every (item, chain) pair: finish the WOTS+ chain from the
+//                    signature value (wots_pk_from_sig, wots.cu:777-789)
+//   k_verify_root    thread per item: T_len over the chain ends, then the
+//                    subtree root from the auth path (sign.cu:3103-3109);
+//                    with L = -1 it computes the FORS key T_k instead, and at
+//                    L = d-1 it compares with PK.root (sign.cu:3116)
+// ---------------------------------------------------------------------------
+template <class HF>
+__global__ void k_verify_root(SetParams P, VerifyArgs A, int L) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    extern __shared__ uint32_t smem[];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.count) return;
+    const SignWork wk = A.work[i];
+    if (wk.flags) {
+        if (L == P.d - 1) A.verdict[i] = -1;
+        return;
+    }
+    const uint8_t *pkb = A.pk.row(i);
+    KeyRegs<N> key;
+    key_from_work<HF>(key, pkb, pkb, wk);
+    uint32_t *tb = smem + threadIdx.x * HF::kSmemWords;
+    uint32_t root[W];
+    typename HF::TStream ts;
+    if (L < 0) {
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_tree(pa, wk.tree);
+        adrs_keypair(pa, wk.idx_leaf);
+        adrs_type(pa, ADDR_FORSPK);
+        HF::t_init(ts, tb, key, pa);
+        for (int t = 0; t < P.k; t++) {
+            uint32_t v[W];
+            HF::load(v, A.fors_roots + ((uint64_t)i * P.k + t) * N);
+            HF::t_absorb(ts, v, key);
+        }
+        HF::t_final(root, ts);
+    } else {
+        uint64_t tree_L;
+        uint32_t idx_L;
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_layer(pa, L);
+        adrs_tree(pa, tree_L);
+        adrs_keypair(pa, idx_L);
+        adrs_type(pa, ADDR_WOTSPK);
+        HF::t_init(ts, tb, key, pa);
+        const uint8_t *wp = A.wpk + (uint64_t)i * LEN * N;
+        for (int c = 0; c < LEN; c++) {
+            uint32_t v[W];
+            HF::load(v, wp + (uint64_t)c * N);
+            HF::t_absorb(ts, v, key);
+        }
+        uint32_t leaf[W];
+        HF::t_final(leaf, ts);
+        Adrs ta;
+        adrs_zero(ta);
+        adrs_layer(ta, L);
+        adrs_tree(ta, tree_L);
+        adrs_type(ta, ADDR_HASHTREE);
+        const uint8_t *auth = A.sig + (uint64_t)i * A.sig_stride + N + P.fors_bytes +
+                              (uint64_t)L * (P.wots_bytes + P.hp * N) + P.wots_bytes;
+        compute_root<HF>(root, leaf, idx_L, 0, auth, P.hp, ta, key);
+    }
+    if (L == P.d - 1) {
+        uint32_t pr[W];
+        HF::load(pr, pkb + N);
+        bool ok = true;
+#pragma unroll
+        for (int x = 0; x < W; x++) ok &= pr[x] == root[x];
+        A.verdict[i] = ok ? 0 : -1;
+    } else {
+        HF::store(A.cur_root + (uint64_t)i * N, root);
+    }
+}
+
+// One warp owns a contiguous range of `per_warp` (item, chain) tasks.  Every
+// lane runs one F step per iteration; a lane whose chain is finished stores
+// it and claims the next task of the range (ballot + prefix count), so the
+// warp advances at the average chain length rather than the longest one.
+template <class HF>
+__global__ void k_verify_chains(SetParams P, VerifyArgs A, int L, int per_warp) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t total = (uint64_t)A.count * LEN;
+    const uint64_t base = gw * (uint64_t)per_warp;
+    if (base >= total) return;
+    const uint64_t end = base + per_warp < total ? base + per_warp : total;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+
+    bool have = false;
+    uint32_t s = 15, item = 0;
+    int c = 0;
+    uint32_t v[W];
+    Adrs wa;
+    typename HF::FCtx fc;
+    KeyRegs<N> key;
+    uint64_t next = base;
+
+    while (true) {
+        // retire finished chains and claim new tasks until every lane either
+        // has a chain with steps left or the range is exhausted
+        while (true) {
+            if (have && s >= 15) {
+                HF::store(A.wpk + ((uint64_t)item * LEN + c) * N, v);
+                have = false;
+            }
+            const uint32_t need = __ballot_sync(0xffffffffu, !have);
+            const uint64_t t = next + __popc(need & lt_mask);
+            if (!have && t < end) {
+                item = (uint32_t)(t / LEN);
+                c = (int)(t % LEN);
+                const SignWork wk = A.work[item];
+                if (wk.flags) {
+                    s = 15;   // rejected item: nothing to compute or store
+                    have = false;
+                } else {
+                    const uint8_t *pkb = A.pk.row(item);
+                    key_from_work<HF>(key, pkb, pkb, wk);
+                    uint64_t tree_L;
+                    uint32_t idx_L;
+                    layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+                    uint32_t root[W];
+                    HF::load(root, A.cur_root + (uint64_t)item * N);
+                    s = chain_len<HF>(P, root, c);
+                    adrs_zero(wa);
+                    adrs_layer(wa, L);
+                    adrs_tree(wa, tree_L);
+                    adrs_type(wa, ADDR_WOTS);
+                    adrs_keypair(wa, idx_L);
+                    adrs_chain(wa, c);
+                    HF::f_prepare(fc, wa, key);
+                    HF::load(v, A.sig + (uint64_t)item * A.sig_stride + N + P.fors_bytes +
+                                    (uint64_t)L * (P.wots_bytes + P.hp * N) + (uint64_t)c * N);
+                    have = true;
+                }
+            }
+            next += __popc(need);
+            // keep refilling while a lane holds a finished (zero-step) chain,
+            // or a lane is idle and the range still has tasks
+            const bool again = __any_sync(0xffffffffu, have && s >= 15) ||
+                               (__any_sync(0xffffffffu, !have) && next < end);
+            if (!again) break;
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+        if (have) {
+            HF::f_step(v, v, fc, s, key);
+            s++;
+        }
+    }
 }
 
 }  // namespace cuspx

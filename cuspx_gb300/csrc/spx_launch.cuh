@@ -14,8 +14,10 @@ namespace cuspx {
 struct Tuning {
     int leaf_block = 128;    // threads per block for k_leaves
     int fors_block = 128;    // threads per block for k_fors_sign (multiple of 32)
-    int verify_block = 64;   // threads per block for k_verify_ht
+    int verify_block = 64;   // threads per block for k_verify_root (and k_verify_ht)
     int tree_warps = 4;      // warps per block for k_trees (upper bound)
+    int chains_per_warp = 64;  // (item, chain) tasks per warp in k_verify_chains
+    int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers
 };
 
 struct KeygenArgs {
@@ -29,7 +31,7 @@ struct KeygenArgs {
 // Optional per-kernel timing: an event is recorded on the launch stream
 // after every kernel of a sequence (event 0 before the first).
 struct PhaseTimer {
-    static constexpr int kMax = 16;
+    static constexpr int kMax = 160;
     cudaEvent_t ev[kMax + 1];
     const char *names[kMax];
     int n = 0;
@@ -85,6 +87,7 @@ struct Family {
         if ((e = cudaFuncSetAttribute(k_fors_sign<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_trees<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_verify_ht<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_verify_root<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         return cudaSuccess;
     }
 
@@ -130,8 +133,22 @@ struct Family {
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_verify_fors", s);
         const int b = tu.verify_block;
-        k_verify_ht<HF><<<ceil_div(A.count, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, A);
-        CUSPX_MARK(pt, "k_verify_ht", s);
+        if (tu.verify_mode == 1) {
+            k_verify_ht<HF><<<ceil_div(A.count, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, A);
+            CUSPX_MARK(pt, "k_verify_ht", s);
+            return;
+        }
+        constexpr int LEN = 2 * N + 3;
+        const int pw = tu.chains_per_warp;
+        const uint64_t warps = ((uint64_t)A.count * LEN + pw - 1) / pw;
+        for (int L = -1; L < P.d; L++) {
+            if (L >= 0) {
+                k_verify_chains<HF><<<ceil_div(warps, 4), 128, 0, s>>>(P, A, L, pw);
+                CUSPX_MARK(pt, "k_verify_chains", s);
+            }
+            k_verify_root<HF><<<ceil_div(A.count, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, A, L);
+            CUSPX_MARK(pt, "k_verify_root", s);
+        }
     }
 
     static void keygen(const SetParams &P, const KeygenArgs &K, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {

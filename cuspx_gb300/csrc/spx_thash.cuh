@@ -166,6 +166,85 @@ struct Sha2 {
         thash<2 * W>(out, k, a, t);
     }
 
+    // ---- WOTS+ chain steps ------------------------------------------------
+    // Along one chain the ADRS differs only in its hash byte (byte 21, in
+    // message word 5), so rounds 0..4 of every F compression -- and rounds
+    // 0..W+4 of the robust mask compression -- are the same for all steps.
+    // f_prepare runs them once; f_step starts each compression after them.
+    struct FCtx {
+        uint32_t st[8];     // state after rounds 0..4 from the midstate
+        uint32_t m[5];      // ADRS words 0..4
+        uint32_t a5;        // ADRS word 5 without the hash byte
+        uint32_t mst[ROBUST ? 8 : 1];   // robust: mask state after rounds 0..W+4 from the IV
+    };
+    SPX_DEV static void f_prepare(FCtx &f, const Adrs &a, const KeyRegs<N> &k) {
+        uint32_t w[16];
+#pragma unroll
+        for (int i = 0; i < 5; i++) f.m[i] = w[i] = a.w[i];
+        f.a5 = a.w[5] & 0xff000000u;
+#pragma unroll
+        for (int i = 0; i < 8; i++) f.st[i] = k.mid[i];
+        sha256_rounds<0, 5>(f.st, w);
+        if (ROBUST) {
+            uint32_t x[16];
+#pragma unroll
+            for (int i = 0; i < W; i++) x[i] = k.pub[i];
+#pragma unroll
+            for (int i = 0; i < 5; i++) x[W + i] = a.w[i];
+            sha256_iv(f.mst);
+            sha256_rounds<0, W + 5>(f.mst, x);
+        }
+    }
+    // out = F(in) at hash address `hash` of the prepared chain
+    SPX_DEV static void f_step(uint32_t out[W], const uint32_t in[W], const FCtx &f, uint32_t hash,
+                               const KeyRegs<N> &k) {
+        const uint32_t a5 = f.a5 | (hash << 16);
+        uint32_t x[W];
+#pragma unroll
+        for (int i = 0; i < W; i++) x[i] = in[i];
+        if (ROBUST) {
+            // bitmask block 0 = SHA256(PUB_SEED || ADRS_c || BE32(0)), resumed after the prefix
+            constexpr int TOT = N + 26;
+            constexpr int NB = (TOT + 9 + 63) / 64;
+            uint32_t mw[16 * NB];
+#pragma unroll
+            for (int i = 0; i < W; i++) mw[i] = k.pub[i];
+#pragma unroll
+            for (int i = 0; i < 5; i++) mw[W + i] = f.m[i];
+            mw[W + 5] = a5;
+            mw[W + 6] = 0x8000u;
+#pragma unroll
+            for (int i = W + 7; i < 16 * NB; i++) mw[i] = 0;
+            mw[16 * NB - 1] = TOT * 8;
+            uint32_t t[8], ms[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) t[i] = f.mst[i];
+            sha256_rounds<W + 5, 64>(t, mw);
+#pragma unroll
+            for (int i = 0; i < 8; i++) ms[i] = t[i] + sha256_iv_word(i);
+            if (NB == 2) sha256_compress(ms, mw + 16);
+#pragma unroll
+            for (int i = 0; i < W; i++) x[i] ^= ms[i];
+        }
+        constexpr int TOT = 22 + N;   // always one block for n <= 32
+        uint32_t m[16];
+#pragma unroll
+        for (int i = 0; i < 5; i++) m[i] = f.m[i];
+        m[5] = a5 | (x[0] >> 16);
+#pragma unroll
+        for (int i = 1; i < W; i++) m[5 + i] = __funnelshift_l(x[i], x[i - 1], 16);
+        m[5 + W] = (x[W - 1] << 16) | 0x8000u;
+#pragma unroll
+        for (int i = 6 + W; i < 16; i++) m[i] = 0;
+        m[15] = (64 + TOT) * 8;
+        uint32_t t[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) t[i] = f.st[i];
+        sha256_rounds<5, 64>(t, m);
+#pragma unroll
+        for (int i = 0; i < W; i++) out[i] = t[i] + k.mid[i];
+    }
+
     // PRF = SHA256(SK_SEED || ADRS_c), no midstate (hash_sha256.cu:65-77)
     SPX_DEV static void PRF(uint32_t out[W], const Adrs &a, const KeyRegs<N> &k) {
         uint32_t m[16];
@@ -432,6 +511,19 @@ struct Shake {
         for (int i = 0; i < W; i++) { t[i] = l[i]; t[W + i] = r[i]; }
         thash<2 * NL>(out, k, a, t);
     }
+    // WOTS+ chain steps: a Keccak permutation has no reusable prefix, so the
+    // prepared chain is just its address
+    struct FCtx {
+        Adrs a;
+    };
+    SPX_DEV static void f_prepare(FCtx &f, const Adrs &a, const KeyRegs<N> &) { f.a = a; }
+    SPX_DEV static void f_step(uint32_t out[W], const uint32_t in[W], const FCtx &f, uint32_t hash,
+                               const KeyRegs<N> &k) {
+        Adrs a = f.a;
+        adrs_hash(a, hash);
+        F(out, in, a, k);
+    }
+
     // PRF = SHAKE256(SK_SEED || ADRS) (hash_shake256.cu:38-47)
     SPX_DEV static void PRF(uint32_t out[W], const Adrs &a, const KeyRegs<N> &k) {
         uint64_t o[NL];

@@ -57,9 +57,20 @@ int cuspx_set_sizes(int set, size_t *pk_bytes, size_t *sk_bytes, size_t *sig_byt
 int cuspx_create(int device, cuspx_ctx **out);
 void cuspx_destroy(cuspx_ctx *ctx);
 const char *cuspx_error(const cuspx_ctx *ctx);
-/* replace the launch mapping of one set (autotuner output); values <= 0 keep defaults */
-int cuspx_set_tuning(cuspx_ctx *ctx, int set, int leaf_block, int fors_block, int verify_block, int tree_warps);
-int cuspx_get_tuning(cuspx_ctx *ctx, int set, int *leaf_block, int *fors_block, int *verify_block, int *tree_warps);
+/* Launch mapping of one parameter set (the autotuner's output).  Replaces
+ * the reference's compile-time knobs (all_option.h:7-68: HP_PARALLELISM,
+ * block-size switches, load-balancing switches). */
+typedef struct {
+    int leaf_block;       /* threads per block, XMSS leaf kernel (multiple of 32) */
+    int fors_block;       /* threads per block, FORS kernel (multiple of 32) */
+    int verify_block;     /* threads per block, per-item verify kernels (multiple of 32) */
+    int tree_warps;       /* warps per block, XMSS tree kernel */
+    int chains_per_warp;  /* (item, chain) tasks per warp, verify chain kernel */
+    int verify_mode;      /* 0 layered verify kernels, 1 one thread per item over all layers */
+} cuspx_tuning;
+/* fields <= 0 (verify_mode < 0) keep the current value */
+int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
+int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
 
 /* ---- one-shot calls on host buffers (synchronous) ----------------------- */
 /* seeds: count x 3n; writes pks: count x 2n, sks: count x 4n

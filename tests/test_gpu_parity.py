@@ -130,3 +130,31 @@ def test_sign_status_flags_bad_key(engine):
     bad[-1] ^= 1
     _, st = engine.sign_batch(sid, [bytes(sk), bytes(bad)], [b"abc", b"abc"])
     assert list(st) == [0, -2]
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-simple", "sha256-192f-robust"])
+def test_verify_mappings_agree(engine, setname):
+    """Every verify launch mapping the autotuner may pick returns the same verdicts."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(99)
+    seeds = [bytes(rng.randrange(256) for _ in range(3 * o.p.n)) for _ in range(3)]
+    pks, sks = engine.keypair_batch(sid, seeds)
+    msgs = [bytes(rng.randrange(256) for _ in range(rng.randrange(0, 300))) for _ in range(12)]
+    kidx = [i % 3 for i in range(12)]
+    sigs, _ = engine.sign_batch(sid, [sks[k] for k in kidx], msgs)
+    sigs = list(sigs)
+    for i in (1, 5, 9):
+        b = bytearray(sigs[i])
+        b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
+        sigs[i] = bytes(b)
+    want = [o.verify(s, m, pks[k]) for s, m, k in zip(sigs, msgs, kidx)]
+    assert want.count(-1) == 3
+    saved = engine.get_tuning(sid)
+    try:
+        for mode, cpw in ((0, 32), (0, 64), (0, 1024), (1, 0)):
+            engine.set_tuning(sid, verify_mode=mode, **({"chains_per_warp": cpw} if cpw else {}))
+            got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
+            assert list(got) == want, (mode, cpw)
+    finally:
+        engine.set_tuning(sid, **saved)

@@ -1,0 +1,134 @@
+"""Host-side checks that need no GPU: the C ABI libraries load and export
+every symbol their headers declare, the parameter-set table matches the
+oracle, the engine's own DRBG/AES match the reference stream, and the
+drop-in size queries answer without a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT, load_golden
+
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def _declared(header):
+    src = open(os.path.join(INCLUDE, header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cuspx_\w+|crypto_sign\w*|randombytes\w*)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import cuspx_gb300
+    return cuspx_gb300.lib()
+
+
+def test_engine_exports_every_declared_symbol(lib):
+    for h in ("cuspx.h", "cuspx_rng.h"):
+        names = _declared(h)
+        assert names, h
+        for name in names:
+            assert hasattr(lib, name), "%s declared in %s but not exported" % (name, h)
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-robust", "sha256-128s-simple"])
+def test_dropin_exports_and_sizes(setname):
+    import cuspx_gb300
+    import spx_oracle
+    L = ctypes.CDLL(cuspx_gb300.dropin_path(setname))
+    for name in _declared("spx_api.h"):
+        assert hasattr(L, name), name
+    o = spx_oracle.Oracle(setname)
+    for fn, want in (("crypto_sign_bytes", o.p.sig_bytes), ("crypto_sign_publickeybytes", o.p.pk_bytes),
+                     ("crypto_sign_secretkeybytes", o.p.sk_bytes), ("crypto_sign_seedbytes", o.p.seed_bytes)):
+        f = getattr(L, fn)
+        f.restype = ctypes.c_ulonglong
+        assert f() == want, fn
+
+
+def test_set_table_matches_oracle():
+    import cuspx_gb300 as c
+    import spx_oracle
+    assert c.num_sets() == 24
+    for sid in range(c.num_sets()):
+        name = c.set_name(sid)
+        o = spx_oracle.Oracle(name)
+        z = c.set_sizes(sid)
+        assert (z["pk"], z["sk"], z["sig"], z["seed"], z["n"]) == \
+            (o.p.pk_bytes, o.p.sk_bytes, o.p.sig_bytes, o.p.seed_bytes, o.p.n), name
+        assert c.set_id(name) == sid
+    assert c.set_id("sha256-128f") == c.set_id("sha256-128f-simple")
+    with pytest.raises(ValueError):
+        c.set_id("sha512-128f")
+
+
+def test_engine_drbg_matches_reference_stream():
+    import cuspx_gb300 as c
+    import spx_oracle
+    g = load_golden("sha256-128f")
+    c.randombytes_init(bytes.fromhex(g["entropy"]))
+    assert c.randombytes(48).hex() == g["drbg_first48"]
+    assert c.randombytes(48).hex() == g["seed"]
+    d = spx_oracle.Drbg(bytes(range(48, 96)))
+    c.randombytes_init(bytes(range(48, 96)))
+    for n in (0, 1, 15, 16, 17, 100):
+        assert c.randombytes(n) == d.bytes(n)
+
+
+def test_engine_aes_known_answers():
+    import cuspx_gb300 as c
+    assert c.aes256_ecb(bytes(range(32)), bytes.fromhex("00112233445566778899aabbccddeeff")).hex() == \
+        "8ea2b7ca516745bfeafc49904b496089"
+    import spx_oracle
+    import random
+    rng = random.Random(3)
+    for _ in range(50):
+        k = bytes(rng.randrange(256) for _ in range(32))
+        p = bytes(rng.randrange(256) for _ in range(16))
+        assert c.aes256_ecb(k, p) == spx_oracle.aes256_ecb(k, p)
+
+
+def test_engine_aes_matches_libcrypto():
+    """The reference DRBG calls OpenSSL's AES-256-ECB (rng.cu:116-136); where the
+    system libcrypto is present, compare against it directly."""
+    import ctypes.util
+    path = ctypes.util.find_library("crypto")
+    if not path:
+        pytest.skip("libcrypto not present")
+    C = ctypes.CDLL(path)
+    C.EVP_CIPHER_CTX_new.restype = ctypes.c_void_p
+    C.EVP_aes_256_ecb.restype = ctypes.c_void_p
+    C.EVP_EncryptInit_ex.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                     ctypes.c_char_p]
+    C.EVP_EncryptUpdate.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
+                                    ctypes.c_char_p, ctypes.c_int]
+    C.EVP_CIPHER_CTX_free.argtypes = [ctypes.c_void_p]
+    import cuspx_gb300 as c
+    import random
+    rng = random.Random(4)
+    for _ in range(20):
+        k = bytes(rng.randrange(256) for _ in range(32))
+        p = bytes(rng.randrange(256) for _ in range(16))
+        ctx = C.EVP_CIPHER_CTX_new()
+        assert C.EVP_EncryptInit_ex(ctx, C.EVP_aes_256_ecb(), None, k, None) == 1
+        out = ctypes.create_string_buffer(32)
+        n = ctypes.c_int()
+        assert C.EVP_EncryptUpdate(ctx, out, ctypes.byref(n), p, 16) == 1
+        C.EVP_CIPHER_CTX_free(ctx)
+        assert out.raw[:16] == c.aes256_ecb(k, p)
+
+
+def test_engine_without_gpu_fails_loudly():
+    """No CPU fallback: on a machine without a usable GPU the engine refuses."""
+    import cuspx_gb300 as c
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = os.path.exists("/dev/nvidia0")
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(c.CuspxError):
+        c.Engine(0)

@@ -339,3 +339,147 @@ def int_peak(device=0, iters=4096):
 def dropin_path(set_name):
     """Path of the NIST api.h drop-in library for one parameter set."""
     return os.path.join(LIB_DIR, "libspx_%s.so" % set_name)
+
+
+# ---------------------------------------------------------------------------
+# serving face (include/cuspx_serve.h)
+# ---------------------------------------------------------------------------
+SUBMIT_BORROW, SUBMIT_DETACH = 1, 2
+E_BUSY, E_TIMEDOUT, E_NOMEM = -4, -5, -3
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("mem_budget", ctypes.c_size_t), ("max_batch", ctypes.c_int), ("max_inflight", ctypes.c_int),
+                ("window_us", ctypes.c_int), ("max_keys", ctypes.c_int), ("max_queue", ctypes.c_size_t)]
+
+
+class ServeCounters(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("submitted", "completed", "refused", "failed", "launches",
+                                                 "sign_done", "verify_done")] + \
+               [("bytes_inflight", ctypes.c_size_t), ("bytes_peak", ctypes.c_size_t)] + \
+               [(f, ctypes.c_double) for f in ("sign_p50_us", "sign_p99_us", "verify_p50_us", "verify_p99_us",
+                                                 "mean_batch")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class LoadgenConfig(ctypes.Structure):
+    _fields_ = [("rate", ctypes.c_double), ("seconds", ctypes.c_double), ("verify_frac", ctypes.c_double),
+                ("nsets", ctypes.c_int), ("sets", ctypes.POINTER(ctypes.c_int)), ("keys_per_set", ctypes.c_uint32),
+                ("min_len", ctypes.c_uint64), ("max_len", ctypes.c_uint64), ("corrupt_frac", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("pool", ctypes.c_int)]
+
+
+class LoadgenResult(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("offered", "completed", "refused", "wrong_verdicts", "sign_done",
+                                                 "verify_done")] + \
+               [(f, ctypes.c_double) for f in ("wall_s", "throughput", "sign_throughput", "verify_throughput",
+                                                 "sign_p50_us", "sign_p99_us", "verify_p50_us", "verify_p99_us",
+                                                 "mean_batch")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+SERVE_EXPORTS = ["cuspx_serve_create", "cuspx_serve_destroy", "cuspx_serve_add_keys", "cuspx_serve_add_pubkeys",
+                 "cuspx_serve_submit", "cuspx_serve_wait", "cuspx_serve_stats", "cuspx_serve_reset_stats",
+                 "cuspx_serve_loadgen"]
+
+
+def _bind_serve(L):
+    if getattr(L, "_serve_bound", False):
+        return L
+    c, vp = ctypes, ctypes.c_void_p
+    L.cuspx_serve_create.argtypes = [vp, c.POINTER(ServeConfig), c.POINTER(vp)]
+    L.cuspx_serve_destroy.argtypes = [vp]
+    L.cuspx_serve_destroy.restype = None
+    L.cuspx_serve_add_keys.argtypes = [vp, c.c_int, c.c_size_t, vp, c.POINTER(c.c_uint32)]
+    L.cuspx_serve_add_pubkeys.argtypes = [vp, c.c_int, c.c_size_t, vp, c.POINTER(c.c_uint32)]
+    L.cuspx_serve_submit.argtypes = [vp, c.c_int, c.c_int, c.c_uint32, vp, c.c_size_t, vp, c.c_size_t, c.c_uint,
+                                     c.POINTER(c.c_uint64)]
+    L.cuspx_serve_wait.argtypes = [vp, c.c_uint64, c.c_long, vp, c.POINTER(c.c_int32), c.POINTER(c.c_double)]
+    L.cuspx_serve_stats.argtypes = [vp, c.POINTER(ServeCounters)]
+    L.cuspx_serve_reset_stats.argtypes = [vp]
+    L.cuspx_serve_loadgen.argtypes = [vp, c.POINTER(LoadgenConfig), c.POINTER(LoadgenResult)]
+    L._serve_bound = True
+    return L
+
+
+class Server:
+    """A serving loop on one engine context (cuspx_serve_*)."""
+
+    def __init__(self, eng, mem_budget=0, max_batch=0, max_inflight=0, window_us=0, max_keys=0, max_queue=0):
+        self.eng = eng
+        self.L = _bind_serve(eng.L)
+        cfg = ServeConfig(mem_budget, max_batch, max_inflight, window_us, max_keys, max_queue)
+        h = ctypes.c_void_p()
+        eng._check(self.L.cuspx_serve_create(eng.h, ctypes.byref(cfg), ctypes.byref(h)), "serve_create")
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            self.L.cuspx_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_keys(self, sid, sks):
+        b = b"".join(bytes(x) for x in sks)
+        first = ctypes.c_uint32()
+        self.eng._check(self.L.cuspx_serve_add_keys(self.h, sid, len(sks), _buf(b), ctypes.byref(first)),
+                        "serve_add_keys")
+        return list(range(first.value, first.value + len(sks)))
+
+    def add_pubkeys(self, sid, pks):
+        b = b"".join(bytes(x) for x in pks)
+        first = ctypes.c_uint32()
+        self.eng._check(self.L.cuspx_serve_add_pubkeys(self.h, sid, len(pks), _buf(b), ctypes.byref(first)),
+                        "serve_add_pubkeys")
+        return list(range(first.value, first.value + len(pks)))
+
+    def submit(self, op, sid, key_id, msg, sig=None):
+        """Returns a ticket, or raises CuspxError with the refusal code."""
+        t = ctypes.c_uint64()
+        msg = bytes(msg)
+        sig = bytes(sig) if sig is not None else None
+        rc = self.L.cuspx_serve_submit(self.h, op, sid, key_id, _buf(msg), len(msg), _buf(sig),
+                                       len(sig) if sig is not None else 0, 0, ctypes.byref(t))
+        if rc != 0:
+            err = CuspxError("serve_submit refused (%d)" % rc)
+            err.code = rc
+            raise err
+        return t.value
+
+    def wait(self, ticket, timeout_us=-1, sig_bytes=0):
+        out = ctypes.create_string_buffer(max(1, sig_bytes))
+        st = ctypes.c_int32()
+        lat = ctypes.c_double()
+        rc = self.L.cuspx_serve_wait(self.h, ticket, timeout_us, _buf(out), ctypes.byref(st), ctypes.byref(lat))
+        if rc != 0:
+            raise CuspxError("serve_wait (%d)" % rc)
+        return (out.raw[:sig_bytes] if sig_bytes else None), st.value, lat.value
+
+    def stats(self):
+        s = ServeCounters()
+        self.L.cuspx_serve_stats(self.h, ctypes.byref(s))
+        return s.as_dict()
+
+    def reset_stats(self):
+        self.L.cuspx_serve_reset_stats(self.h)
+
+    def loadgen(self, rate, seconds, sets, keys_per_set, verify_frac=0.7, min_len=16, max_len=1 << 20,
+                corrupt_frac=0.0, seed=1, pool=64):
+        arr = (ctypes.c_int * len(sets))(*sets)
+        cfg = LoadgenConfig(rate, seconds, verify_frac, len(sets), arr, keys_per_set, min_len, max_len,
+                            corrupt_frac, seed, pool)
+        res = LoadgenResult()
+        rc = self.L.cuspx_serve_loadgen(self.h, ctypes.byref(cfg), ctypes.byref(res))
+        out = res.as_dict()
+        out["rc"] = rc
+        return out

@@ -62,6 +62,16 @@ def build(verbose=False, jobs=None, ptxas_verbose=False):
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
         glob.glob(os.path.join(INC, "*.h"))
     extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+    # extra device flags (A/B experiments); a change of flags rebuilds everything
+    user = os.environ.get("CUSPX_NVCC_FLAGS", "").split()
+    extra += user
+    stamp = os.path.join(BUILD, "flags.stamp")
+    prev = open(stamp).read() if os.path.exists(stamp) else None
+    if prev != " ".join(user):
+        for o in glob.glob(os.path.join(BUILD, "*.o")):
+            os.remove(o)
+        with open(stamp, "w") as f:
+            f.write(" ".join(user))
     steps = []
     fam_src = os.path.join(CSRC, "spx_family.cu")
     for h in (0, 1):

@@ -78,7 +78,8 @@ struct cuspx_ctx {
     std::string err;
     Tuning tune[kNumSets];
     bool configured[2][3][2] = {};
-    std::mutex mu;
+    std::mutex mu;       // one-shot batches
+    std::mutex cfg_mu;   // kernel attribute configuration
     cuspx_batch *oneshot[3][kNumSets] = {};
 };
 
@@ -107,9 +108,12 @@ struct cuspx_batch {
     uint8_t *wpk = nullptr, *cur_root = nullptr;
     size_t count = 0;
     bool use_keyrow = false, use_aux = false, use_siglen = false;
+    const uint8_t *bound_keys = nullptr;   // external device key table (not owned)
+    size_t bound_nkeys = 0;
     cudaGraphExec_t gexec = nullptr;
     size_t g_count = 0;
     bool g_keyrow = false, g_aux = false, g_siglen = false;
+    const uint8_t *g_keys = nullptr;
     Tuning g_tune{};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     bool ran = false;
@@ -258,9 +262,12 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
     CK(cudaSetDevice(ctx->device), ctx);
     const SetDesc &sd = kSets[set];
     FamilyOps &ops = g_family[sd.hash][sd.n / 8 - 2][sd.robust];
-    if (!ctx->configured[sd.hash][sd.n / 8 - 2][sd.robust]) {
-        CK(ops.configure(), ctx);
-        ctx->configured[sd.hash][sd.n / 8 - 2][sd.robust] = true;
+    {
+        std::lock_guard<std::mutex> lk(ctx->cfg_mu);
+        if (!ctx->configured[sd.hash][sd.n / 8 - 2][sd.robust]) {
+            CK(ops.configure(), ctx);
+            ctx->configured[sd.hash][sd.n / 8 - 2][sd.robust] = true;
+        }
     }
     cuspx_batch *b = new cuspx_batch();
     b->ctx = ctx;
@@ -341,7 +348,8 @@ int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t
     const SetParams &P = b->P;
     const size_t n = P.n;
     if (count > b->cap) return fail(ctx, CUSPX_EINVAL, "upload: count exceeds batch capacity");
-    if (count && !keys) return fail(ctx, CUSPX_EINVAL, "upload: keys is null");
+    const bool bound = b->bound_keys != nullptr && b->op != CUSPX_OP_KEYGEN;
+    if (count && !keys && !bound) return fail(ctx, CUSPX_EINVAL, "upload: keys is null");
     CK(cudaSetDevice(ctx->device), ctx);
     if (b->op == CUSPX_OP_KEYGEN) {
         // seeds (count x 3n) into the first 3n bytes of each sk row
@@ -349,8 +357,9 @@ int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t
         b->count = count;
         return CUSPX_OK;
     }
+    if (bound && !keys) nkeys = b->bound_nkeys;
     if (nkeys == 0) nkeys = count;
-    if (nkeys > b->key_cap) return fail(ctx, CUSPX_EINVAL, "upload: more keys than key capacity");
+    if (!bound && nkeys > b->key_cap) return fail(ctx, CUSPX_EINVAL, "upload: more keys than key capacity");
     if (key_index) {
         for (size_t i = 0; i < count; i++)
             if (key_index[i] >= nkeys) return fail(ctx, CUSPX_EINVAL, "upload: key_index out of range");
@@ -365,7 +374,8 @@ int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t
     }
     if (msg_bytes > b->msg_cap) return fail(ctx, CUSPX_EINVAL, "upload: messages exceed message capacity");
     const size_t krow = b->op == CUSPX_OP_VERIFY ? 2 * n : 4 * n;
-    if (nkeys) CK(cudaMemcpyAsync(b->keys, keys, nkeys * krow, cudaMemcpyHostToDevice, b->s), ctx);
+    if (keys && bound) return fail(ctx, CUSPX_EINVAL, "upload: batch is bound to a resident key table");
+    if (nkeys && keys) CK(cudaMemcpyAsync(b->keys, keys, nkeys * krow, cudaMemcpyHostToDevice, b->s), ctx);
     if (key_index && count) CK(cudaMemcpyAsync(b->keyrow, key_index, count * 4, cudaMemcpyHostToDevice, b->s), ctx);
     if (msg_bytes) CK(cudaMemcpyAsync(b->msg, msgs, msg_bytes, cudaMemcpyHostToDevice, b->s), ctx);
     if (count) {
@@ -394,7 +404,8 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
     if (b->op == CUSPX_OP_SIGN) {
         SignArgs A;
         A.count = cnt;
-        A.sk = KeyRef{b->keys, b->use_keyrow ? b->keyrow : nullptr, (uint32_t)P.sk_bytes};
+        A.sk = KeyRef{b->bound_keys ? b->bound_keys : b->keys, b->use_keyrow ? b->keyrow : nullptr,
+                      (uint32_t)P.sk_bytes};
         A.msg = MsgRef{b->msg, b->off, b->len};
         A.optrand = b->use_aux ? b->aux : nullptr;
         A.sig = b->out;
@@ -408,7 +419,8 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
     } else if (b->op == CUSPX_OP_VERIFY) {
         VerifyArgs A;
         A.count = cnt;
-        A.pk = KeyRef{b->keys, b->use_keyrow ? b->keyrow : nullptr, (uint32_t)P.pk_bytes};
+        A.pk = KeyRef{b->bound_keys ? b->bound_keys : b->keys, b->use_keyrow ? b->keyrow : nullptr,
+                      (uint32_t)P.pk_bytes};
         A.msg = MsgRef{b->msg, b->off, b->len};
         A.sig = b->aux;
         A.sig_stride = P.sig_bytes;
@@ -460,7 +472,7 @@ int cuspx_batch_run(cuspx_batch *b) {
     }
     const Tuning &tu = ctx->tune[b->set];
     const bool stale = !b->gexec || b->g_count != b->count || b->g_keyrow != b->use_keyrow ||
-                       b->g_aux != b->use_aux || b->g_siglen != b->use_siglen ||
+                       b->g_aux != b->use_aux || b->g_siglen != b->use_siglen || b->g_keys != b->bound_keys ||
                        memcmp(&b->g_tune, &tu, sizeof(Tuning)) != 0;
     if (stale) {
         if (b->gexec) {
@@ -478,6 +490,7 @@ int cuspx_batch_run(cuspx_batch *b) {
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
         b->g_count = b->count;
+        b->g_keys = b->bound_keys;
         b->g_tune = tu;
         b->g_keyrow = b->use_keyrow;
         b->g_aux = b->use_aux;
@@ -497,22 +510,28 @@ int cuspx_batch_sync(cuspx_batch *b) {
     return CUSPX_OK;
 }
 
-int cuspx_batch_download(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status) {
+int cuspx_batch_download_async(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status) {
     if (!b) return CUSPX_EINVAL;
     cuspx_ctx *ctx = b->ctx;
     const SetParams &P = b->P;
-    CK(cudaSetDevice(ctx->device), ctx);
     const size_t cnt = b->count;
-    if (cnt) {
-        if (b->op == CUSPX_OP_SIGN) {
-            if (out) CK(cudaMemcpyAsync(out, b->out, cnt * P.sig_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
-        } else if (b->op == CUSPX_OP_KEYGEN) {
-            if (out) CK(cudaMemcpyAsync(out, b->keys, cnt * P.sk_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
-            if (out2) CK(cudaMemcpyAsync(out2, b->out, cnt * P.pk_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
-        }
-        if (status && b->op != CUSPX_OP_KEYGEN)
-            CK(cudaMemcpyAsync(status, b->status, cnt * 4, cudaMemcpyDeviceToHost, b->s), ctx);
+    if (!cnt) return CUSPX_OK;
+    if (b->op == CUSPX_OP_SIGN) {
+        if (out) CK(cudaMemcpyAsync(out, b->out, cnt * P.sig_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
+    } else if (b->op == CUSPX_OP_KEYGEN) {
+        if (out) CK(cudaMemcpyAsync(out, b->keys, cnt * P.sk_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
+        if (out2) CK(cudaMemcpyAsync(out2, b->out, cnt * P.pk_bytes, cudaMemcpyDeviceToHost, b->s), ctx);
     }
+    if (status && b->op != CUSPX_OP_KEYGEN)
+        CK(cudaMemcpyAsync(status, b->status, cnt * 4, cudaMemcpyDeviceToHost, b->s), ctx);
+    return CUSPX_OK;
+}
+
+int cuspx_batch_download(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status) {
+    if (!b) return CUSPX_EINVAL;
+    CK(cudaSetDevice(b->ctx->device), b->ctx);
+    int rc = cuspx_batch_download_async(b, out, out2, status);
+    if (rc) return rc;
     return cuspx_batch_sync(b);
 }
 
@@ -524,6 +543,13 @@ int cuspx_batch_last_ms(cuspx_batch *b, float *ms) {
 }
 
 void *cuspx_batch_stream(cuspx_batch *b) { return b ? (void *)b->s : nullptr; }
+
+int cuspx_batch_bind_keys(cuspx_batch *b, const void *d_keys, size_t nkeys) {
+    if (!b || b->op == CUSPX_OP_KEYGEN) return CUSPX_EINVAL;
+    b->bound_keys = (const uint8_t *)d_keys;
+    b->bound_nkeys = d_keys ? nkeys : 0;
+    return CUSPX_OK;
+}
 
 int cuspx_batch_device_ptrs(cuspx_batch *b, void **keys, void **msgs, void **msg_off, void **msg_len, void **aux,
                             void **out, void **status) {

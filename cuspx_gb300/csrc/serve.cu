@@ -1,0 +1,632 @@
+// serve.cu -- the serving face (include/cuspx_serve.h): resident keys,
+// continuous batching over several in-flight launches per (operation, set),
+// memory-budgeted admission, per-request latency, and an open-loop Poisson
+// load generator.
+//
+// Threads: callers submit and wait under one mutex; a single scheduler
+// thread owns every CUDA call on the serving batches (pack into pinned
+// staging, upload, graph launch, asynchronous download, completion by event
+// query), so batch objects are never shared between threads.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <random>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cuspx.h"
+#include "../../include/cuspx_serve.h"
+#include "spx_kernels.cuh"
+#include "spx_sets.h"
+
+namespace cuspx {
+SetParams make_params(const SetDesc &s);
+}
+using namespace cuspx;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct Req {
+    uint64_t ticket = 0;
+    int op = 0, set = 0;
+    uint32_t key = 0;
+    const uint8_t *msg = nullptr;
+    size_t mlen = 0;
+    std::vector<uint8_t> msg_own;
+    const uint8_t *sig = nullptr;
+    size_t siglen = 0;
+    std::vector<uint8_t> sig_own;
+    std::vector<uint8_t> out;
+    int32_t status = 0;
+    int32_t expect = 1;     // load generator: expected verdict (1 = none)
+    bool done = false;
+    unsigned flags = 0;
+    Clock::time_point t0, t1;
+};
+
+struct KeyTable {
+    size_t cap = 0, n = 0;
+    uint8_t *d_sk = nullptr, *d_pk = nullptr;
+    std::vector<uint8_t> has_sk;
+};
+
+struct Slot {
+    cuspx_batch *b = nullptr;
+    size_t cap = 0, msg_cap = 0;
+    uint8_t *h_msg = nullptr;
+    uint64_t *h_off = nullptr, *h_len = nullptr, *h_siglen = nullptr;
+    uint32_t *h_kidx = nullptr;
+    uint8_t *h_aux = nullptr, *h_out = nullptr;
+    int32_t *h_status = nullptr;
+    cudaEvent_t ev = nullptr;
+    bool busy = false;
+    size_t bytes = 0;
+    std::vector<Req *> reqs;
+};
+
+struct Group {
+    int op = 0, set = 0;
+    std::deque<Req *> pending;
+    std::vector<Slot *> slots;
+    size_t per_item = 0;
+    SetParams P{};
+};
+
+double percentile(std::vector<float> v, double q) {
+    if (v.empty()) return 0.0;
+    size_t k = (size_t)std::min<double>(v.size() - 1, std::floor(q * (v.size() - 1) + 0.5));
+    std::nth_element(v.begin(), v.begin() + k, v.end());
+    return v[k];
+}
+
+}  // namespace
+
+struct cuspx_server {
+    cuspx_ctx *ctx = nullptr;
+    cuspx_serve_config cfg{};
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done;
+    std::thread th;
+    bool stop = false;
+    std::vector<KeyTable> keys;
+    std::vector<Group> groups;   // index (op - 1) * kNumSets + set
+    std::unordered_map<uint64_t, Req *> live;
+    uint64_t next_ticket = 1;
+    size_t pending_total = 0, bytes_inflight = 0, bytes_peak = 0, bytes_alloc = 0;
+    uint64_t submitted = 0, completed = 0, refused = 0, failed = 0, launches = 0, batched = 0;
+    uint64_t sign_done = 0, verify_done = 0, wrong = 0;
+    std::vector<float> lat_sign, lat_verify;
+    Clock::time_point last_done;
+};
+
+static size_t item_bytes(int op, const SetParams &P) {
+    const size_t n = P.n;
+    size_t b = sizeof(SignWork) + P.k * n + 64;
+    if (op == CUSPX_OP_SIGN)
+        b += P.sig_bytes + n + (size_t)P.d * ((size_t)1 << P.hp) * n + P.d * n + (size_t)P.d * P.len * 16 * n;
+    else
+        b += P.sig_bytes + 8 + (size_t)P.len * n + n;
+    return b;
+}
+
+static void free_slot(Slot *sl) {
+    if (sl->b) cuspx_batch_destroy(sl->b);
+    cudaFreeHost(sl->h_msg);
+    cudaFreeHost(sl->h_off);
+    cudaFreeHost(sl->h_len);
+    cudaFreeHost(sl->h_siglen);
+    cudaFreeHost(sl->h_kidx);
+    cudaFreeHost(sl->h_aux);
+    cudaFreeHost(sl->h_out);
+    cudaFreeHost(sl->h_status);
+    if (sl->ev) cudaEventDestroy(sl->ev);
+    delete sl;
+}
+
+// (re)size a slot for `cap` items and `msg_cap` message bytes
+static bool size_slot(cuspx_server *s, Group &g, Slot *sl, size_t cap, size_t msg_cap) {
+    const SetParams &P = g.P;
+    if (sl->b && sl->cap >= cap && sl->msg_cap >= msg_cap) return true;
+    cap = std::max(cap, sl->cap);
+    msg_cap = std::max<size_t>(std::max(msg_cap, sl->msg_cap), 1 << 20);
+    if (sl->b) {
+        cuspx_batch_destroy(sl->b);
+        sl->b = nullptr;
+    }
+    if (cuspx_batch_create(s->ctx, g.op, g.set, cap, msg_cap, 1, &sl->b) != CUSPX_OK) return false;
+    const KeyTable &kt = s->keys[g.set];
+    cuspx_batch_bind_keys(sl->b, g.op == CUSPX_OP_SIGN ? kt.d_sk : kt.d_pk, kt.cap);
+    auto host = [](void **p, size_t bytes) { cudaFreeHost(*p); return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };
+    bool ok = host((void **)&sl->h_msg, msg_cap + 64) && host((void **)&sl->h_off, cap * 8) &&
+              host((void **)&sl->h_len, cap * 8) && host((void **)&sl->h_siglen, cap * 8) &&
+              host((void **)&sl->h_kidx, cap * 4) &&
+              host((void **)&sl->h_aux, g.op == CUSPX_OP_VERIFY ? cap * P.sig_bytes : 16) &&
+              host((void **)&sl->h_out, g.op == CUSPX_OP_SIGN ? cap * P.sig_bytes : 16) &&
+              host((void **)&sl->h_status, cap * 4);
+    if (!sl->ev) cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming);
+    sl->cap = cap;
+    sl->msg_cap = msg_cap;
+    return ok;
+}
+
+// pack requests into the slot's pinned staging and launch asynchronously
+static bool launch_slot(cuspx_server *s, Group &g, Slot *sl) {
+    const SetParams &P = g.P;
+    size_t total = 0;
+    for (Req *r : sl->reqs) total += (r->mlen + 15) & ~(size_t)15;
+    if (!size_slot(s, g, sl, sl->reqs.size(), total)) return false;
+    size_t off = 0;
+    for (size_t i = 0; i < sl->reqs.size(); i++) {
+        Req *r = sl->reqs[i];
+        sl->h_off[i] = off;
+        sl->h_len[i] = r->mlen;
+        sl->h_kidx[i] = r->key;
+        if (r->mlen) memcpy(sl->h_msg + off, r->msg, r->mlen);
+        off += (r->mlen + 15) & ~(size_t)15;
+        if (g.op == CUSPX_OP_VERIFY) {
+            uint8_t *row = sl->h_aux + i * P.sig_bytes;
+            const size_t take = std::min<size_t>(r->siglen, P.sig_bytes);
+            memcpy(row, r->sig, take);
+            if (take < (size_t)P.sig_bytes) memset(row + take, 0, P.sig_bytes - take);
+            sl->h_siglen[i] = r->siglen;
+        }
+    }
+    const size_t cnt = sl->reqs.size();
+    if (cuspx_batch_upload(sl->b, cnt, nullptr, 0, sl->h_kidx, sl->h_msg, off, sl->h_off, sl->h_len,
+                           g.op == CUSPX_OP_VERIFY ? sl->h_aux : nullptr,
+                           g.op == CUSPX_OP_VERIFY ? sl->h_siglen : nullptr) != CUSPX_OK)
+        return false;
+    if (cuspx_batch_run(sl->b) != CUSPX_OK) return false;
+    if (cuspx_batch_download_async(sl->b, g.op == CUSPX_OP_SIGN ? sl->h_out : nullptr, nullptr, sl->h_status) !=
+        CUSPX_OK)
+        return false;
+    return cudaEventRecord(sl->ev, (cudaStream_t)cuspx_batch_stream(sl->b)) == cudaSuccess;
+}
+
+// mark a slot's requests done (called with the lock held)
+static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
+    const SetParams &P = g.P;
+    const auto now = Clock::now();
+    for (size_t i = 0; i < sl->reqs.size(); i++) {
+        Req *r = sl->reqs[i];
+        r->status = ok ? sl->h_status[i] : -3;
+        if (!ok) s->failed++;
+        if (g.op == CUSPX_OP_SIGN && ok && !(r->flags & CUSPX_SUBMIT_DETACH))
+            r->out.assign(sl->h_out + i * P.sig_bytes, sl->h_out + (i + 1) * P.sig_bytes);
+        r->t1 = now;
+        r->done = true;
+        const float us = std::chrono::duration<float, std::micro>(now - r->t0).count();
+        if (g.op == CUSPX_OP_SIGN) {
+            s->lat_sign.push_back(us);
+            s->sign_done++;
+        } else {
+            s->lat_verify.push_back(us);
+            s->verify_done++;
+        }
+        if (r->expect != 1 && r->status != r->expect) s->wrong++;
+        s->completed++;
+        if (r->flags & CUSPX_SUBMIT_DETACH) {
+            s->live.erase(r->ticket);
+            delete r;
+        }
+    }
+    s->last_done = now;
+    sl->reqs.clear();
+    s->bytes_inflight -= sl->bytes;
+    sl->bytes = 0;
+    sl->busy = false;
+}
+
+static void scheduler(cuspx_server *s) {
+    cudaSetDevice(s->device);
+    const auto window = std::chrono::microseconds(s->cfg.window_us);
+    const auto drain_deadline_len = std::chrono::seconds(60);
+    Clock::time_point drain_deadline{};
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        // ---- retire finished launches ----
+        bool any_busy = false;
+        for (Group &g : s->groups) {
+            for (Slot *sl : g.slots) {
+                if (!sl->busy) continue;
+                cudaError_t e = cudaEventQuery(sl->ev);
+                if (e == cudaErrorNotReady) {
+                    any_busy = true;
+                    continue;
+                }
+                finish_slot(s, g, sl, e == cudaSuccess);
+                s->cv_done.notify_all();
+            }
+        }
+        if (s->stop) {
+            if (drain_deadline == Clock::time_point{}) drain_deadline = Clock::now() + drain_deadline_len;
+            if ((!any_busy && s->pending_total == 0) || Clock::now() > drain_deadline) break;
+        }
+        // ---- admit new launches ----
+        const auto now = Clock::now();
+        Clock::time_point next_wake = now + std::chrono::microseconds(50);
+        for (Group &g : s->groups) {
+            while (!g.pending.empty()) {
+                int inflight = 0;
+                Slot *free_sl = nullptr;
+                for (Slot *sl : g.slots) {
+                    if (sl->busy) inflight++;
+                    else if (!free_sl) free_sl = sl;
+                }
+                const bool full = g.pending.size() >= (size_t)s->cfg.max_batch;
+                const bool waited = now - g.pending.front()->t0 >= window;
+                if (!(full || waited || inflight == 0)) {
+                    next_wake = std::min(next_wake, g.pending.front()->t0 + window);
+                    break;
+                }
+                if (!free_sl) {
+                    if ((int)g.slots.size() >= s->cfg.max_inflight) break;
+                    free_sl = new Slot();
+                    g.slots.push_back(free_sl);
+                }
+                // take as many as fit the batch size and the memory budget
+                size_t n = 0, bytes = 0;
+                for (Req *r : g.pending) {
+                    if (n == (size_t)s->cfg.max_batch) break;
+                    const size_t add = g.per_item + ((r->mlen + 15) & ~(size_t)15);
+                    if (s->bytes_inflight + bytes + add > s->cfg.mem_budget && n > 0) break;
+                    if (s->bytes_inflight + bytes + add > s->cfg.mem_budget && s->bytes_inflight > 0) break;
+                    bytes += add;
+                    n++;
+                }
+                if (n == 0) break;   // budget full: wait for completions
+                for (size_t i = 0; i < n; i++) {
+                    free_sl->reqs.push_back(g.pending.front());
+                    g.pending.pop_front();
+                }
+                s->pending_total -= n;
+                free_sl->busy = true;
+                free_sl->bytes = bytes;
+                s->bytes_inflight += bytes;
+                s->bytes_peak = std::max(s->bytes_peak, s->bytes_inflight);
+                s->launches++;
+                s->batched += n;
+                lk.unlock();
+                const bool ok = launch_slot(s, g, free_sl);
+                lk.lock();
+                if (!ok) {
+                    finish_slot(s, g, free_sl, false);
+                    s->cv_done.notify_all();
+                }
+            }
+        }
+        s->cv_sched.wait_until(lk, next_wake);
+    }
+}
+
+extern "C" {
+
+int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_server **out) {
+    if (!ctx || !out) return CUSPX_EINVAL;
+    cuspx_server *s = new cuspx_server();
+    s->ctx = ctx;
+    if (cfg) s->cfg = *cfg;
+    if (!s->cfg.mem_budget) s->cfg.mem_budget = (size_t)8 << 30;
+    if (s->cfg.max_batch <= 0) s->cfg.max_batch = 1024;
+    if (s->cfg.max_inflight <= 0) s->cfg.max_inflight = 3;
+    if (s->cfg.window_us <= 0) s->cfg.window_us = 500;
+    if (s->cfg.max_keys <= 0) s->cfg.max_keys = 4096;
+    if (!s->cfg.max_queue) s->cfg.max_queue = 1u << 20;
+    cudaGetDevice(&s->device);
+    s->keys.resize(kNumSets);
+    s->groups.resize(2 * kNumSets);
+    for (int op = 1; op <= 2; op++)
+        for (int set = 0; set < kNumSets; set++) {
+            Group &g = s->groups[(op - 1) * kNumSets + set];
+            g.op = op;
+            g.set = set;
+            g.P = make_params(kSets[set]);
+            g.per_item = item_bytes(op, g.P);
+        }
+    s->th = std::thread(scheduler, s);
+    *out = s;
+    return CUSPX_OK;
+}
+
+void cuspx_serve_destroy(cuspx_server *s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_sched.notify_all();
+    if (s->th.joinable()) s->th.join();
+    for (Group &g : s->groups) {
+        for (Slot *sl : g.slots) {
+            if (sl->busy && sl->b) cuspx_batch_sync(sl->b);
+            free_slot(sl);
+        }
+        for (Req *r : g.pending) delete r;
+    }
+    for (auto &kv : s->live)
+        if (kv.second->done) delete kv.second;   // completed but never waited for
+    for (KeyTable &kt : s->keys) {
+        cudaFree(kt.d_sk);
+        cudaFree(kt.d_pk);
+    }
+    delete s;
+}
+
+static int add_rows(cuspx_server *s, int set, size_t count, const uint8_t *rows, bool secret, uint32_t *first) {
+    if (!s || set < 0 || set >= kNumSets || (count && !rows)) return CUSPX_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    KeyTable &kt = s->keys[set];
+    const size_t n = kSets[set].n;
+    if (!kt.d_sk) {
+        kt.cap = s->cfg.max_keys;
+        if (cudaMalloc(&kt.d_sk, kt.cap * 4 * n) != cudaSuccess || cudaMalloc(&kt.d_pk, kt.cap * 2 * n) != cudaSuccess)
+            return CUSPX_ENOMEM;
+        cudaMemset(kt.d_sk, 0, kt.cap * 4 * n);
+        cudaMemset(kt.d_pk, 0, kt.cap * 2 * n);
+    }
+    if (kt.n + count > kt.cap) return CUSPX_ENOMEM;
+    for (size_t i = 0; i < count; i++) {
+        const uint8_t *r = rows + i * (secret ? 4 * n : 2 * n);
+        if (secret) {
+            if (cudaMemcpy(kt.d_sk + (kt.n + i) * 4 * n, r, 4 * n, cudaMemcpyHostToDevice)) return CUSPX_ECUDA;
+            if (cudaMemcpy(kt.d_pk + (kt.n + i) * 2 * n, r + 2 * n, 2 * n, cudaMemcpyHostToDevice)) return CUSPX_ECUDA;
+        } else {
+            if (cudaMemcpy(kt.d_pk + (kt.n + i) * 2 * n, r, 2 * n, cudaMemcpyHostToDevice)) return CUSPX_ECUDA;
+        }
+        kt.has_sk.push_back(secret ? 1 : 0);
+    }
+    if (first) *first = (uint32_t)kt.n;
+    kt.n += count;
+    return CUSPX_OK;
+}
+
+int cuspx_serve_add_keys(cuspx_server *s, int set, size_t count, const uint8_t *sks, uint32_t *first_id) {
+    return add_rows(s, set, count, sks, true, first_id);
+}
+
+int cuspx_serve_add_pubkeys(cuspx_server *s, int set, size_t count, const uint8_t *pks, uint32_t *first_id) {
+    return add_rows(s, set, count, pks, false, first_id);
+}
+
+static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8_t *msg, size_t mlen,
+                  const uint8_t *sig, size_t siglen, unsigned flags, int32_t expect, uint64_t *ticket) {
+    if (!s || (op != CUSPX_OP_SIGN && op != CUSPX_OP_VERIFY) || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    if (mlen && !msg) return CUSPX_EINVAL;
+    if (op == CUSPX_OP_VERIFY && siglen && !sig) return CUSPX_EINVAL;
+    Req *r = new Req();
+    r->op = op;
+    r->set = set;
+    r->key = key_id;
+    r->flags = flags;
+    r->expect = expect;
+    if (flags & CUSPX_SUBMIT_BORROW) {
+        r->msg = msg;
+        r->sig = sig;
+    } else {
+        r->msg_own.assign(msg, msg + mlen);
+        r->msg = r->msg_own.data();
+        if (op == CUSPX_OP_VERIFY) {
+            r->sig_own.assign(sig, sig + siglen);
+            r->sig = r->sig_own.data();
+        }
+    }
+    r->mlen = mlen;
+    r->siglen = op == CUSPX_OP_VERIFY ? siglen : 0;
+    std::unique_lock<std::mutex> lk(s->mu);
+    const KeyTable &kt = s->keys[set];
+    Group &g = s->groups[(op - 1) * kNumSets + set];
+    int rc = CUSPX_OK;
+    if (s->stop) rc = CUSPX_EBUSY;
+    else if (key_id >= kt.n || (op == CUSPX_OP_SIGN && !kt.has_sk[key_id])) rc = CUSPX_EINVAL;
+    else if (g.per_item + mlen > s->cfg.mem_budget) rc = CUSPX_ENOMEM;
+    else if (s->pending_total >= s->cfg.max_queue) rc = CUSPX_EBUSY;
+    if (rc != CUSPX_OK) {
+        s->refused++;
+        lk.unlock();
+        delete r;
+        return rc;
+    }
+    r->ticket = s->next_ticket++;
+    r->t0 = Clock::now();
+    s->live[r->ticket] = r;
+    g.pending.push_back(r);
+    s->pending_total++;
+    s->submitted++;
+    if (ticket) *ticket = r->ticket;
+    const bool kick = g.pending.size() == 1 || g.pending.size() >= (size_t)s->cfg.max_batch;
+    lk.unlock();
+    if (kick) s->cv_sched.notify_one();
+    return CUSPX_OK;
+}
+
+int cuspx_serve_submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8_t *msg, size_t mlen,
+                       const uint8_t *sig, size_t siglen, unsigned flags, uint64_t *ticket) {
+    return submit(s, op, set, key_id, msg, mlen, sig, siglen, flags, 1, ticket);
+}
+
+int cuspx_serve_wait(cuspx_server *s, uint64_t ticket, long timeout_us, uint8_t *sig_out, int32_t *status,
+                     double *latency_us) {
+    if (!s) return CUSPX_EINVAL;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->live.find(ticket);
+    if (it == s->live.end()) return CUSPX_EINVAL;
+    Req *r = it->second;
+    auto pred = [&] { return r->done; };
+    if (timeout_us < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), pred)) return CUSPX_ETIMEDOUT;
+    if (sig_out && !r->out.empty()) memcpy(sig_out, r->out.data(), r->out.size());
+    if (status) *status = r->status;
+    if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(r->t1 - r->t0).count();
+    s->live.erase(it);
+    delete r;
+    return CUSPX_OK;
+}
+
+int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st) {
+    if (!s || !st) return CUSPX_EINVAL;
+    std::vector<float> ls, lv;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        st->submitted = s->submitted;
+        st->completed = s->completed;
+        st->refused = s->refused;
+        st->failed = s->failed;
+        st->launches = s->launches;
+        st->sign_done = s->sign_done;
+        st->verify_done = s->verify_done;
+        st->bytes_inflight = s->bytes_inflight;
+        st->bytes_peak = s->bytes_peak;
+        st->mean_batch = s->launches ? (double)s->batched / s->launches : 0.0;
+        ls = s->lat_sign;
+        lv = s->lat_verify;
+    }
+    st->sign_p50_us = percentile(ls, 0.50);
+    st->sign_p99_us = percentile(ls, 0.99);
+    st->verify_p50_us = percentile(lv, 0.50);
+    st->verify_p99_us = percentile(lv, 0.99);
+    return CUSPX_OK;
+}
+
+int cuspx_serve_reset_stats(cuspx_server *s) {
+    if (!s) return CUSPX_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->submitted = s->completed = s->refused = s->failed = s->launches = s->batched = 0;
+    s->sign_done = s->verify_done = s->wrong = 0;
+    s->bytes_peak = s->bytes_inflight;
+    s->lat_sign.clear();
+    s->lat_verify.clear();
+    return CUSPX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// open-loop Poisson load generator
+// ---------------------------------------------------------------------------
+int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_loadgen_result *out) {
+    if (!s || !c || !out || c->nsets <= 0 || !c->sets || c->rate <= 0 || c->seconds <= 0 || c->keys_per_set == 0 ||
+        c->min_len > c->max_len)
+        return CUSPX_EINVAL;
+    std::mt19937_64 rng(c->seed);
+    const size_t buf_len = c->max_len + 4096;
+    std::vector<uint8_t> buf(buf_len);
+    for (auto &x : buf) x = (uint8_t)rng();
+    const double lmin = std::log((double)std::max<uint64_t>(1, c->min_len));
+    const double lmax = std::log((double)std::max<uint64_t>(1, c->max_len));
+    auto draw_len = [&]() -> size_t {
+        std::uniform_real_distribution<double> u(lmin, lmax);
+        size_t L = (size_t)std::floor(std::exp(u(rng)));
+        return std::min<size_t>(std::max<size_t>(L, c->min_len), c->max_len);
+    };
+    auto draw_off = [&](size_t L) -> size_t { return (size_t)(rng() % (buf_len - L + 1)); };
+
+    // pre-signed pool per set for verify requests (and a corrupted twin of each)
+    const int pool = std::max(1, c->pool);
+    struct Entry {
+        const uint8_t *m;
+        size_t mlen;
+        uint32_t key;
+        std::vector<uint8_t> sig, bad;
+    };
+    std::vector<std::vector<Entry>> pools(c->nsets);
+    for (int si = 0; si < c->nsets; si++) {
+        const int set = c->sets[si];
+        size_t sigb = 0;
+        cuspx_set_sizes(set, nullptr, nullptr, &sigb, nullptr, nullptr);
+        std::vector<uint64_t> tickets(pool);
+        pools[si].resize(pool);
+        for (int i = 0; i < pool; i++) {
+            Entry &e = pools[si][i];
+            e.mlen = draw_len();
+            e.m = buf.data() + draw_off(e.mlen);
+            e.key = (uint32_t)(rng() % c->keys_per_set);
+            e.sig.resize(sigb);
+            int rc = submit(s, CUSPX_OP_SIGN, set, e.key, e.m, e.mlen, nullptr, 0, CUSPX_SUBMIT_BORROW, 1, &tickets[i]);
+            if (rc) return rc;
+        }
+        for (int i = 0; i < pool; i++) {
+            Entry &e = pools[si][i];
+            int32_t st = 0;
+            int rc = cuspx_serve_wait(s, tickets[i], 120000000L, e.sig.data(), &st, nullptr);
+            if (rc || st) return rc ? rc : CUSPX_ECUDA;
+            e.bad = e.sig;
+            const size_t pos = (size_t)(rng() % sigb);
+            e.bad[pos] ^= (uint8_t)(1u << (rng() % 8));
+        }
+    }
+    cuspx_serve_reset_stats(s);
+
+    std::exponential_distribution<double> gap(c->rate);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    uint64_t offered = 0, refused = 0;
+    const auto t0 = Clock::now();
+    double t_next = 0.0;
+    while (true) {
+        t_next += gap(rng);
+        if (t_next >= c->seconds) break;
+        const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(t_next));
+        while (true) {
+            auto now = Clock::now();
+            if (now >= due) break;
+            if (due - now > std::chrono::microseconds(200)) std::this_thread::sleep_for(due - now - std::chrono::microseconds(100));
+            else std::this_thread::yield();
+        }
+        const int si = (int)(rng() % c->nsets);
+        const int set = c->sets[si];
+        int rc;
+        offered++;
+        if (U(rng) < c->verify_frac) {
+            const Entry &e = pools[si][rng() % pool];
+            const bool corrupt = U(rng) < c->corrupt_frac;
+            const std::vector<uint8_t> &sg = corrupt ? e.bad : e.sig;
+            rc = submit(s, CUSPX_OP_VERIFY, set, e.key, e.m, e.mlen, sg.data(), sg.size(),
+                        CUSPX_SUBMIT_BORROW | CUSPX_SUBMIT_DETACH, corrupt ? -1 : 0, nullptr);
+        } else {
+            const size_t L = draw_len();
+            rc = submit(s, CUSPX_OP_SIGN, set, (uint32_t)(rng() % c->keys_per_set), buf.data() + draw_off(L), L,
+                        nullptr, 0, CUSPX_SUBMIT_BORROW | CUSPX_SUBMIT_DETACH, 1, nullptr);
+        }
+        if (rc) refused++;
+    }
+    // drain (bounded)
+    const auto deadline = Clock::now() + std::chrono::seconds(120);
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        s->cv_done.wait_until(lk, deadline, [&] { return s->completed >= offered - refused; });
+    }
+    cuspx_serve_counters st;
+    cuspx_serve_stats(s, &st);
+    double wall;
+    uint64_t wrong;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        wall = std::chrono::duration<double>(s->last_done - t0).count();
+        wrong = s->wrong;
+    }
+    out->offered = offered;
+    out->completed = st.completed;
+    out->refused = refused;
+    out->wrong_verdicts = wrong;
+    out->sign_done = st.sign_done;
+    out->verify_done = st.verify_done;
+    out->wall_s = wall;
+    out->throughput = wall > 0 ? st.completed / wall : 0;
+    out->sign_throughput = wall > 0 ? st.sign_done / wall : 0;
+    out->verify_throughput = wall > 0 ? st.verify_done / wall : 0;
+    out->sign_p50_us = st.sign_p50_us;
+    out->sign_p99_us = st.sign_p99_us;
+    out->verify_p50_us = st.verify_p50_us;
+    out->verify_p99_us = st.verify_p99_us;
+    out->mean_batch = st.mean_batch;
+    return st.completed + refused == offered ? CUSPX_OK : CUSPX_ETIMEDOUT;
+}
+
+}  // extern "C"

@@ -90,6 +90,23 @@ __host__ __device__ constexpr uint32_t sha256_iv_word(int i) {
 
 SPX_DEV uint32_t rotr(uint32_t x, int c) { return __funnelshift_r(x, x, c); }
 
+// Pipe balancing.  The compression is bound by the ALU pipe (funnel
+// shifts, LOP3 and IADD3 all issue there) while the FMA pipe idles.  An add
+// written as a * c_one + b with c_one an opaque constant-bank 1 must issue as
+// IMAD on the FMA pipe, so the 2-input adds (e = d + t1 each round, the last
+// add of each schedule word) move there.  CUSPX_FMA_ADDS=0 restores plain adds.
+#ifndef CUSPX_FMA_ADDS
+#define CUSPX_FMA_ADDS 1
+#endif
+static __constant__ uint32_t c_one = 1u;
+SPX_DEV uint32_t add_fma(uint32_t a, uint32_t b) {
+#if CUSPX_FMA_ADDS
+    return a * c_one + b;
+#else
+    return a + b;
+#endif
+}
+
 SPX_DEV void sha256_iv(uint32_t s[8]) {
 #pragma unroll
     for (int i = 0; i < 8; i++) s[i] = sha256_iv_word(i);
@@ -109,14 +126,14 @@ SPX_DEV void sha256_rounds(uint32_t st[8], uint32_t w[16]) {
             uint32_t x = w[(i - 15) & 15], y = w[(i - 2) & 15];
             uint32_t s0 = rotr(x, 7) ^ rotr(x, 18) ^ (x >> 3);
             uint32_t s1 = rotr(y, 17) ^ rotr(y, 19) ^ (y >> 10);
-            wi = w[i & 15] = w[i & 15] + s0 + w[(i - 7) & 15] + s1;
+            wi = w[i & 15] = add_fma(w[i & 15], s0 + w[(i - 7) & 15] + s1);
         }
         uint32_t t1 = h + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g)) + sha256_k(i) + wi;
         uint32_t t2 = (rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22)) + ((a & b) | (c & (a | b)));
         h = g;
         g = f;
         f = e;
-        e = d + t1;
+        e = add_fma(d, t1);
         d = c;
         c = b;
         b = a;

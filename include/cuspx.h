@@ -110,11 +110,20 @@ int cuspx_batch_run(cuspx_batch *b);
 /* sign -> out = sigs; verify -> out unused (verdicts in status);
  * keygen -> out = sk rows, out2 = pk rows */
 int cuspx_batch_download(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status);
+/* same copies, enqueued on the batch stream without waiting (host buffers
+ * must be pinned for the copies to overlap; completion by cuspx_batch_sync
+ * or an event recorded on cuspx_batch_stream) */
+int cuspx_batch_download_async(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status);
 int cuspx_batch_sync(cuspx_batch *b);
 /* device time of the last run, from CUDA events recorded on the batch stream */
 int cuspx_batch_last_ms(cuspx_batch *b, float *ms);
 /* the batch's cudaStream_t */
 void *cuspx_batch_stream(cuspx_batch *b);
+/* Use a device-resident key table (nkeys rows of sk for sign, pk for verify,
+ * owned by the caller and kept alive while the batch uses it) instead of
+ * uploading keys; upload() is then called with keys = NULL and a key_index.
+ * Pass d_keys = NULL to unbind. */
+int cuspx_batch_bind_keys(cuspx_batch *b, const void *d_keys, size_t nkeys);
 /* device pointers of the batch buffers (for device-resident callers) */
 int cuspx_batch_device_ptrs(cuspx_batch *b, void **keys, void **msgs, void **msg_off, void **msg_len, void **aux,
                             void **out, void **status);

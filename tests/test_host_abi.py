@@ -26,7 +26,7 @@ def lib():
 
 
 def test_engine_exports_every_declared_symbol(lib):
-    for h in ("cuspx.h", "cuspx_rng.h"):
+    for h in ("cuspx.h", "cuspx_rng.h", "cuspx_serve.h"):
         names = _declared(h)
         assert names, h
         for name in names:

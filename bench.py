@@ -156,6 +156,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the uneven-mixed and verify-heavy workloads")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run one sign and one verify batch of this many messages (for ncu) and exit")
     ap.add_argument("--profile-set", default=SET)
@@ -311,6 +312,10 @@ def main():
     served = None
     if rank == 0 and not args.no_served:
         served = served_runs(c, eng)
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        extra["uneven_mixed"] = uneven_mixed(c, eng)
+        extra["verify_heavy"] = verify_heavy(c, eng)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -346,6 +351,7 @@ def main():
         if plain:
             line["plain"] = plain
             line["batched_vs_plain"] = value / plain["sign_per_s"] if plain["sign_per_s"] else None
+        line.update(extra)
         if served:
             line.update(served)
             ok = [p for p in served["served_128f"] if p["sign_p99_ms"] < 20.0 and p["wrong_verdicts"] == 0]
@@ -413,6 +419,106 @@ def served_runs(c, eng, seconds=2.0):
     srv.close()
     out["served_stream"] = {"sets": names, "keys": per * len(sids), "lengths": "log-uniform 16 B..1 MiB",
                             "points": pts}
+    return out
+
+
+def uneven_mixed(c, eng, reps=3):
+    """Uneven batch: 256 distinct keypairs (128 per set), 2048 sign requests,
+    lengths floor(exp(U(ln 1, ln 65536))) B, sets SHA-256-128s-simple and
+    SHA-256-192f-robust drawn 50/50, autotuned mapping, one graph launch."""
+    import numpy as np
+    from cuspx_gb300 import autotune
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+    names = ["sha256-128s-simple", "sha256-192f-robust"]
+    sids = [c.set_id(n) for n in names]
+    rng = np.random.default_rng(33)
+    keys = {}
+    tuned = {}
+    for n, sid in zip(names, sids):
+        z = c.set_sizes(sid)
+        pks, sks = eng.keypair_batch(sid, [rng.bytes(z["seed"]) for _ in range(128)])
+        keys[sid] = sks
+        tuned[n] = autotune.tune(eng, sid, c.OP_SIGN, count=1024, mlen=64)[0]
+    set_ids, sks, msgs = [], [], []
+    for _ in range(2048):
+        sid = sids[int(rng.integers(0, 2))]
+        L = int(np.floor(np.exp(rng.uniform(0.0, np.log(65536.0)))))
+        set_ids.append(sid)
+        sks.append(keys[sid][int(rng.integers(0, 128))])
+        msgs.append(rng.bytes(L))
+    ms = c.MixedSigner(eng)
+    sigs, st, _ = ms.sign(set_ids, sks, msgs)
+    times = []
+    for _ in range(reps):
+        _, _, dev = ms.sign(set_ids, sks, msgs)
+        times.append(dev)
+    ms.close()
+    # byte-compare a seeded subset against the CPU oracle
+    chk = [int(i) for i in np.random.default_rng(34).choice(2048, 6, replace=False)]
+    ok = all(st == 0)
+    for i in chk:
+        o = spx_oracle.Oracle(c.set_name(set_ids[i]))
+        ok &= sigs[i] == o.sign(msgs[i], sks[i])
+    best = min(times)
+    return {"workload": "2048 sign requests, 256 keys, lengths log-uniform 1 B..64 KiB, sets %s 50/50, one "
+                        "graph launch" % "+".join(names),
+            "sign_per_s": 2048 / (best / 1e3), "ms_per_launch": best, "tuning": tuned,
+            "oracle_subset_identical": bool(ok), "subset": len(chk)}
+
+
+def verify_heavy(c, eng, reps=3):
+    """16384 SHAKE-256-256f signatures (simple and robust) over 256-B
+    messages, 10% with one seeded random byte xored with a nonzero byte; every
+    verdict must be the expected one and a subset must match the CPU oracle."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+    out = {}
+    for name in ("shake256-256f-simple", "shake256-256f-robust"):
+        sid = c.set_id(name)
+        z = c.set_sizes(sid)
+        rng = np.random.default_rng(44)
+        count = 16384
+        pks, sks = eng.keypair_batch(sid, [rng.bytes(z["seed"]) for _ in range(16)])
+        kidx = (np.arange(count) % 16).astype(np.uint32)
+        msgs = rng.integers(0, 256, size=(count, 256), dtype=np.uint8)
+        slab = np.ascontiguousarray(msgs.reshape(-1))
+        offs = np.arange(count, dtype=np.uint64) * 256
+        lens = np.full(count, 256, dtype=np.uint64)
+        skb = np.frombuffer(b"".join(sks), dtype=np.uint8).copy()
+        pkb = np.frombuffer(b"".join(pks), dtype=np.uint8).copy()
+        sb = eng.batch(c.OP_SIGN, sid, count, slab.nbytes, 16)
+        sb.upload(count, skb, 16, kidx, slab, slab.nbytes, offs, lens)
+        sb.run()
+        sigs = np.zeros(count * z["sig"], dtype=np.uint8)
+        st = np.zeros(count, dtype=np.int32)
+        sb.download(sigs, None, st)
+        sb.close()
+        bad = rng.random(count) < 0.10
+        for i in np.nonzero(bad)[0]:
+            pos = int(rng.integers(0, z["sig"]))
+            sigs[i * z["sig"] + pos] ^= np.uint8(int(rng.integers(1, 256)))
+        vb = eng.batch(c.OP_VERIFY, sid, count, slab.nbytes, 16)
+        vb.upload(count, pkb, 16, kidx, slab, slab.nbytes, offs, lens, sigs)
+        times = []
+        for _ in range(reps + 1):
+            vb.run()
+            vb.sync()
+            times.append(vb.last_ms())
+        v = np.zeros(count, dtype=np.int32)
+        vb.download(None, None, v)
+        vb.close()
+        expect = np.where(bad, -1, 0)
+        o = spx_oracle.Oracle(name)
+        sub = [int(i) for i in np.random.default_rng(45).choice(count, 48, replace=False)] + \
+              [int(i) for i in np.nonzero(bad)[0][:16]]
+        oracle_ok = all(o.verify(sigs[i * z["sig"]:(i + 1) * z["sig"]].tobytes(), msgs[i].tobytes(),
+                                 pks[int(kidx[i])]) == int(v[i]) for i in sub)
+        best = min(times[1:])
+        out[name] = {"verify_per_s": count / (best / 1e3), "ms_per_launch": best, "corrupted": int(bad.sum()),
+                     "all_verdicts_expected": bool((v == expect).all()), "oracle_subset_agrees": bool(oracle_ok),
+                     "oracle_subset": len(sub)}
     return out
 
 

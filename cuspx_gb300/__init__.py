@@ -38,7 +38,7 @@ class CuspxError(RuntimeError):
 class Tuning(ctypes.Structure):
     """cuspx_tuning: the launch mapping of one parameter set."""
     _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
-                                            "chains_per_warp", "verify_mode")]
+                                            "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -188,7 +188,7 @@ class Engine:
 
     def set_tuning(self, sid, **kw):
         """Change fields of a set's launch mapping (others keep their value)."""
-        t = Tuning(0, 0, 0, 0, 0, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")
@@ -483,3 +483,71 @@ class Server:
         out = res.as_dict()
         out["rc"] = rc
         return out
+
+
+# ---------------------------------------------------------------------------
+# mixed parameter sets in one graph launch (cuspx_group_run)
+# ---------------------------------------------------------------------------
+def _bind_group(L):
+    if not getattr(L, "_group_bound", False):
+        L.cuspx_group_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_float)]
+        L._group_bound = True
+    return L
+
+
+def group_run(eng, batches):
+    """Run several uploaded batches as one CUDA graph; returns device ms."""
+    L = _bind_group(eng.L)
+    arr = (ctypes.c_void_p * len(batches))(*[b.h.value for b in batches])
+    ms = ctypes.c_float()
+    eng._check(L.cuspx_group_run(eng.h, arr, len(batches), ctypes.byref(ms)), "group_run")
+    return ms.value
+
+
+class MixedSigner:
+    """Sign requests of several parameter sets, each with its own key, in one
+    graph launch: requests are grouped per set into device-resident batches
+    (keys uploaded once per batch) that run concurrently in one graph."""
+
+    def __init__(self, eng):
+        self.eng = eng
+        self.batches = {}
+
+    def sign(self, set_ids, sks, msgs, optrand=None):
+        import numpy as np
+        order = {}
+        for i, sid in enumerate(set_ids):
+            order.setdefault(sid, []).append(i)
+        runs = []
+        for sid, idx in order.items():
+            z = set_sizes(sid)
+            slab, offs, lens = pack_messages([msgs[i] for i in idx])
+            keys = b"".join(bytes(sks[i]) for i in idx)
+            cap = len(idx)
+            b = self.batches.get(sid)
+            if b is None or b._cap < cap or b._mcap < len(slab):
+                if b is not None:
+                    b.close()
+                b = self.eng.batch(OP_SIGN, sid, max(cap, 1), max(len(slab), 1 << 16), max(cap, 1))
+                b._cap, b._mcap = max(cap, 1), max(len(slab), 1 << 16)
+                self.batches[sid] = b
+            opt = b"".join(bytes(optrand[i]) for i in idx) if optrand is not None else None
+            b.upload(cap, keys, cap, None, slab, len(slab), offs, lens, opt)
+            runs.append((sid, idx, b, z))
+        ms = group_run(self.eng, [r[2] for r in runs])
+        sigs = [None] * len(msgs)
+        status = np.zeros(len(msgs), dtype=np.int32)
+        for sid, idx, b, z in runs:
+            out = np.zeros(len(idx) * z["sig"], dtype=np.uint8)
+            st = np.zeros(len(idx), dtype=np.int32)
+            b.download(out, None, st)
+            for j, i in enumerate(idx):
+                sigs[i] = out[j * z["sig"]:(j + 1) * z["sig"]].tobytes()
+                status[i] = st[j]
+        return sigs, status, ms
+
+    def close(self):
+        for b in self.batches.values():
+            b.close()
+        self.batches = {}

@@ -81,6 +81,17 @@ struct cuspx_ctx {
     std::mutex mu;       // one-shot batches
     std::mutex cfg_mu;   // kernel attribute configuration
     cuspx_batch *oneshot[3][kNumSets] = {};
+    // multi-batch (mixed parameter set) graphs
+    struct GroupGraph {
+        std::vector<cuspx_batch *> batches;
+        std::vector<size_t> counts;
+        std::vector<Tuning> tunes;
+        cudaGraphExec_t exec;
+        cudaStream_t origin;
+        cudaEvent_t e0, e1;
+    };
+    std::vector<GroupGraph> groups;
+    std::mutex group_mu;
 };
 
 struct ProfEntry {
@@ -110,11 +121,27 @@ struct cuspx_batch {
     bool use_keyrow = false, use_aux = false, use_siglen = false;
     const uint8_t *bound_keys = nullptr;   // external device key table (not owned)
     size_t bound_nkeys = 0;
-    cudaGraphExec_t gexec = nullptr;
-    size_t g_count = 0;
-    bool g_keyrow = false, g_aux = false, g_siglen = false;
-    const uint8_t *g_keys = nullptr;
-    Tuning g_tune{};
+    // captured launch sequences keyed by everything baked into them; an item
+    // count seen for the first time launches directly and is captured on
+    // its second use
+    struct GraphKey {
+        size_t count;
+        bool keyrow, aux, siglen;
+        const uint8_t *keys;
+        Tuning tune;
+        bool operator==(const GraphKey &o) const {
+            return count == o.count && keyrow == o.keyrow && aux == o.aux && siglen == o.siglen && keys == o.keys &&
+                   memcmp(&tune, &o.tune, sizeof(Tuning)) == 0;
+        }
+    };
+    struct GraphEntry {
+        GraphKey key;
+        cudaGraphExec_t exec;
+        uint64_t last_use;
+    };
+    std::vector<GraphEntry> graphs;
+    std::vector<GraphKey> seen;
+    uint64_t use_clock = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     bool ran = false;
     bool profile = false;
@@ -186,6 +213,13 @@ int cuspx_create(int device, cuspx_ctx **out) {
 
 void cuspx_destroy(cuspx_ctx *ctx) {
     if (!ctx) return;
+    for (auto &g : ctx->groups) {
+        cudaStreamSynchronize(g.origin);
+        cudaGraphExecDestroy(g.exec);
+        cudaEventDestroy(g.e0);
+        cudaEventDestroy(g.e1);
+        cudaStreamDestroy(g.origin);
+    }
     for (auto &row : ctx->oneshot)
         for (auto *b : row)
             if (b) cuspx_batch_destroy(b);
@@ -222,6 +256,14 @@ int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
         if (in->verify_mode > 1) return fail(ctx, CUSPX_EINVAL, "verify_mode must be 0 or 1");
         t.verify_mode = in->verify_mode;
     }
+    if (in->fors_lanes_log2 >= 0) {
+        if (in->fors_lanes_log2 > 5) return fail(ctx, CUSPX_EINVAL, "fors_lanes_log2 must be in 0..5");
+        t.fors_lanes_log2 = in->fors_lanes_log2;
+    }
+    if (in->tree_mode >= 0) {
+        if (in->tree_mode > 1) return fail(ctx, CUSPX_EINVAL, "tree_mode must be 0 or 1");
+        t.tree_mode = in->tree_mode;
+    }
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->tune[set] = t;   // batches re-capture their graph when the mapping changed
     return CUSPX_OK;
@@ -236,6 +278,8 @@ int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
     out->tree_warps = t.tree_warps;
     out->chains_per_warp = t.chains_per_warp;
     out->verify_mode = t.verify_mode;
+    out->fors_lanes_log2 = t.fors_lanes_log2;
+    out->tree_mode = t.tree_mode;
     return CUSPX_OK;
 }
 
@@ -330,7 +374,7 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
 void cuspx_batch_destroy(cuspx_batch *b) {
     if (!b) return;
     if (b->s) cudaStreamSynchronize(b->s);
-    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
     for (void *p : b->allocs) cudaFree(p);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
@@ -471,33 +515,49 @@ int cuspx_batch_run(cuspx_batch *b) {
         return CUSPX_OK;
     }
     const Tuning &tu = ctx->tune[b->set];
-    const bool stale = !b->gexec || b->g_count != b->count || b->g_keyrow != b->use_keyrow ||
-                       b->g_aux != b->use_aux || b->g_siglen != b->use_siglen || b->g_keys != b->bound_keys ||
-                       memcmp(&b->g_tune, &tu, sizeof(Tuning)) != 0;
-    if (stale) {
-        if (b->gexec) {
-            cudaGraphExecDestroy(b->gexec);
-            b->gexec = nullptr;
+    cuspx_batch::GraphKey key{b->count, b->use_keyrow, b->use_aux, b->use_siglen, b->bound_keys, tu};
+    b->use_clock++;
+    cuspx_batch::GraphEntry *hit = nullptr;
+    for (auto &g : b->graphs)
+        if (g.key == key) hit = &g;
+    if (!hit) {
+        const bool second = std::find(b->seen.begin(), b->seen.end(), key) != b->seen.end();
+        if (!second) {
+            // first use of this shape: launch directly, remember it
+            if (b->seen.size() >= 64) b->seen.erase(b->seen.begin());
+            b->seen.push_back(key);
+            CK(cudaEventRecord(b->e0, b->s), ctx);
+            launch_seq(b, nullptr);
+            CK(cudaGetLastError(), ctx);
+            CK(cudaEventRecord(b->e1, b->s), ctx);
+            b->ran = true;
+            return CUSPX_OK;
         }
         cudaGraph_t g;
+        cudaGraphExec_t exec = nullptr;
         CK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal), ctx);
         launch_seq(b, nullptr);
         cudaError_t le = cudaGetLastError();
         cudaError_t ce = cudaStreamEndCapture(b->s, &g);
         if (le != cudaSuccess) return cuda_fail(ctx, le, "launch during capture");
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
-        cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
-        b->g_count = b->count;
-        b->g_keys = b->bound_keys;
-        b->g_tune = tu;
-        b->g_keyrow = b->use_keyrow;
-        b->g_aux = b->use_aux;
-        b->g_siglen = b->use_siglen;
+        if (b->graphs.size() >= 8) {
+            auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                        [](const cuspx_batch::GraphEntry &x, const cuspx_batch::GraphEntry &y) {
+                                            return x.last_use < y.last_use;
+                                        });
+            cudaGraphExecDestroy(lru->exec);
+            b->graphs.erase(lru);
+        }
+        b->graphs.push_back(cuspx_batch::GraphEntry{key, exec, 0});
+        hit = &b->graphs.back();
     }
+    hit->last_use = b->use_clock;
     CK(cudaEventRecord(b->e0, b->s), ctx);
-    CK(cudaGraphLaunch(b->gexec, b->s), ctx);
+    CK(cudaGraphLaunch(hit->exec, b->s), ctx);
     CK(cudaEventRecord(b->e1, b->s), ctx);
     b->ran = true;
     return CUSPX_OK;
@@ -675,6 +735,82 @@ int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks
         return rc;
     if ((rc = cuspx_batch_run(b))) return rc;
     return cuspx_batch_download(b, nullptr, nullptr, verdicts);
+}
+
+// ---------------------------------------------------------------------------
+// mixed parameter sets in one graph launch
+// ---------------------------------------------------------------------------
+int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *ms) {
+    if (!ctx || !batches || nb <= 0 || nb > 64) return CUSPX_EINVAL;
+    for (int i = 0; i < nb; i++)
+        if (!batches[i] || batches[i]->ctx != ctx || batches[i]->profile)
+            return fail(ctx, CUSPX_EINVAL, "group_run: batch missing, from another context, or profiling");
+    CK(cudaSetDevice(ctx->device), ctx);
+    std::lock_guard<std::mutex> lk(ctx->group_mu);
+    // the batches' uploads (on their own streams) must be complete before the
+    // streams join a capture or the graph reads their buffers
+    for (int i = 0; i < nb; i++) CK(cudaStreamSynchronize(batches[i]->s), ctx);
+    cuspx_ctx::GroupGraph *hit = nullptr;
+    for (auto &g : ctx->groups) {
+        if ((int)g.batches.size() != nb) continue;
+        bool same = true;
+        for (int i = 0; i < nb && same; i++) {
+            cuspx_batch *b = batches[i];
+            same = g.batches[i] == b && g.counts[i] == b->count &&
+                   memcmp(&g.tunes[i], &ctx->tune[b->set], sizeof(Tuning)) == 0;
+        }
+        if (same) hit = &g;
+    }
+    if (!hit) {
+        cuspx_ctx::GroupGraph gg;
+        gg.batches.assign(batches, batches + nb);
+        for (int i = 0; i < nb; i++) {
+            gg.counts.push_back(batches[i]->count);
+            gg.tunes.push_back(ctx->tune[batches[i]->set]);
+        }
+        CK(cudaStreamCreateWithFlags(&gg.origin, cudaStreamNonBlocking), ctx);
+        cudaEventCreate(&gg.e0);
+        cudaEventCreate(&gg.e1);
+        std::vector<cudaEvent_t> fork(nb + 1), join(nb);
+        for (auto &e : fork) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        for (auto &e : join) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(gg.origin, cudaStreamCaptureModeThreadLocal), ctx);
+        cudaEventRecord(fork[0], gg.origin);
+        for (int i = 0; i < nb; i++) {
+            cudaStreamWaitEvent(batches[i]->s, fork[0], 0);
+            launch_seq(batches[i], nullptr);
+            cudaEventRecord(join[i], batches[i]->s);
+            cudaStreamWaitEvent(gg.origin, join[i], 0);
+        }
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(gg.origin, &graph);
+        for (auto &e : fork) cudaEventDestroy(e);
+        for (auto &e : join) cudaEventDestroy(e);
+        if (le != cudaSuccess) return cuda_fail(ctx, le, "group launch during capture");
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "group cudaStreamEndCapture");
+        cudaError_t ie = cudaGraphInstantiate(&gg.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(ctx, ie, "group cudaGraphInstantiate");
+        if (ctx->groups.size() >= 16) {
+            auto &old = ctx->groups.front();
+            cudaStreamSynchronize(old.origin);
+            cudaGraphExecDestroy(old.exec);
+            cudaEventDestroy(old.e0);
+            cudaEventDestroy(old.e1);
+            cudaStreamDestroy(old.origin);
+            ctx->groups.erase(ctx->groups.begin());
+        }
+        ctx->groups.push_back(gg);
+        hit = &ctx->groups.back();
+    }
+    CK(cudaEventRecord(hit->e0, hit->origin), ctx);
+    CK(cudaGraphLaunch(hit->exec, hit->origin), ctx);
+    CK(cudaEventRecord(hit->e1, hit->origin), ctx);
+    CK(cudaStreamSynchronize(hit->origin), ctx);
+    if (ms) CK(cudaEventElapsedTime(ms, hit->e0, hit->e1), ctx);
+    for (int i = 0; i < nb; i++) batches[i]->ran = false;
+    return CUSPX_OK;
 }
 
 }  // extern "C"

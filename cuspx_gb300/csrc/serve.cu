@@ -134,11 +134,15 @@ static void free_slot(Slot *sl) {
 }
 
 // (re)size a slot for `cap` items and `msg_cap` message bytes
+// Slots are sized once for a full batch; the message area grows
+// geometrically, so re-creation (whose cudaFree would wait for the whole
+// device) is rare.
 static bool size_slot(cuspx_server *s, Group &g, Slot *sl, size_t cap, size_t msg_cap) {
     const SetParams &P = g.P;
     if (sl->b && sl->cap >= cap && sl->msg_cap >= msg_cap) return true;
-    cap = std::max(cap, sl->cap);
-    msg_cap = std::max<size_t>(std::max(msg_cap, sl->msg_cap), 1 << 20);
+    cap = std::max<size_t>(std::max(cap, sl->cap), (size_t)s->cfg.max_batch);
+    size_t want = std::max<size_t>(sl->msg_cap ? 2 * sl->msg_cap : (size_t)4 << 20, msg_cap);
+    msg_cap = want;
     if (sl->b) {
         cuspx_batch_destroy(sl->b);
         sl->b = nullptr;

@@ -6,12 +6,12 @@
 // batch of thousands of signatures fills all 152 SMs:
 //
 //   k_sign_msg      thread / signature   PRF_msg, H_msg -> R, FORS digest, tree, leaf
-//   k_fors_sign     warp / FORS tree     leaves (PRF+F), per-lane subtree stack,
-//                                        5 shuffle levels, auth path, root
+//   k_fors_sign     2^g lanes / FORS tree leaves (PRF+F), per-lane subtree stack,
+//                                        g shuffle levels, auth path, root
 //   k_leaves        thread / XMSS leaf   WOTS+ key (len chains x 15 F) streamed into
 //                                        T_len; the signing leaf records its chains
 //   k_trees         warp / XMSS tree     level-by-level reduction in shared memory,
-//                                        auth path, root
+//                                        auth path, root (k_trees_lane: lane / tree)
 //   k_sign_finish   block / signature    FORS pk (T_k), WOTS signatures gathered
 //                                        from the recorded chains
 //
@@ -171,27 +171,36 @@ __global__ void k_sign_msg(SetParams P, SignArgs A) {
 }
 
 // ===========================================================================
-// FORS sign: one warp per (signature, tree).  Lane l owns the contiguous
-// subtree of 2^(a-5) leaves starting at l*2^(a-5) and reduces it with a
-// shared-memory stack (treehash, utils.cu:189-241); the 32 subtree roots are
-// then reduced over 5 shuffle levels.  Auth-path nodes are written by
-// whichever lane holds them.
+// FORS sign: a group of G = 2^g lanes per (signature, tree), g in 0..5.  Lane
+// l of a group owns the contiguous subtree of 2^(a-g) leaves starting at
+// l*2^(a-g) and reduces it with a shared-memory stack (treehash,
+// utils.cu:189-241); the G subtree roots are then reduced over g shuffle
+// levels inside the group.  g = 0 is one lane per tree (no idle lanes in the
+// reduction, best for big batches); g = 5 is one warp per tree (lowest
+// latency, best for few signatures or tall trees).  Auth-path nodes are
+// written by whichever lane holds them.
 // ===========================================================================
 template <class HF>
-__global__ void k_fors_sign(SetParams P, SignArgs A) {
+__global__ void k_fors_sign(SetParams P, SignArgs A, int g) {
     constexpr int W = HF::W, N = 4 * W;
     extern __shared__ uint32_t smem[];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= (uint64_t)A.count * P.k) return;
-    const uint32_t item = (uint32_t)(gw / P.k);
-    const int t = (int)(gw % P.k);
+    const uint32_t G = 1u << g;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = (uint32_t)(gid & (G - 1));
+    uint64_t tid = gid >> g;
+    const uint64_t ntrees = (uint64_t)A.count * P.k;
+    // every lane of a warp takes part in the shuffles; lanes past the end work
+    // on tree 0 and store nothing
+    const bool valid = tid < ntrees;
+    if (!valid) tid = 0;
+    const uint32_t item = (uint32_t)(tid / P.k);
+    const int t = (int)(tid % P.k);
     const SignWork wk = A.work[item];
     const uint8_t *sk = A.sk.row(item);
     KeyRegs<N> key;
     key_from_work<HF>(key, sk, sk + 2 * N, wk);
     const uint32_t idx = fors_index(wk.mhash, P.a, t);
-    const int sub = P.a - 5;                    // lane subtree height
+    const int sub = P.a - g;                    // lane subtree height
     const uint32_t per = 1u << sub;
     const uint32_t off = (uint32_t)t << P.a;   // idx_offset
     uint8_t *sigt = A.sig + (uint64_t)item * P.sig_bytes + N + (uint64_t)t * (P.a + 1) * N;
@@ -202,9 +211,9 @@ __global__ void k_fors_sign(SetParams P, SignArgs A) {
     adrs_keypair(ad, wk.idx_leaf);
     adrs_type(ad, ADDR_FORSTREE);
 
-    // per-lane stack: (sub+1) entries of W words, plus heights
-    uint32_t *stk = smem + threadIdx.x * (P.a - 4) * W;   // sub+1 entries
-    int heights[16];
+    // per-lane stack: sub+1 entries of W words (heights in registers/local)
+    uint32_t *stk = smem + threadIdx.x * (sub + 1) * W;
+    int heights[17];
     int sp = 0;
     uint32_t v[W];
     for (uint32_t jj = 0; jj < per; jj++) {
@@ -213,9 +222,9 @@ __global__ void k_fors_sign(SetParams P, SignArgs A) {
         adrs_index(ad, off + j);
         uint32_t skv[W];
         HF::PRF(skv, ad, key);
-        if (j == idx) HF::store(sigt, skv);
+        if (valid && j == idx) HF::store(sigt, skv);
         HF::F(v, skv, ad, key);
-        if ((idx ^ 1u) == j) HF::store(sigt + N, v);
+        if (valid && (idx ^ 1u) == j) HF::store(sigt + N, v);
         int hgt = 0;
         // merge equal-height nodes on the stack
         while (sp > 0 && heights[sp - 1] == hgt) {
@@ -228,7 +237,7 @@ __global__ void k_fors_sign(SetParams P, SignArgs A) {
             HF::H(v, l, v, ad, key);
             sp--;
             hgt++;
-            if (((idx >> hgt) ^ 1u) == tidx) HF::store(sigt + N + (uint64_t)hgt * N, v);
+            if (valid && ((idx >> hgt) ^ 1u) == tidx) HF::store(sigt + N + (uint64_t)hgt * N, v);
         }
 #pragma unroll
         for (int q = 0; q < W; q++) stk[sp * W + q] = v[q];
@@ -236,21 +245,21 @@ __global__ void k_fors_sign(SetParams P, SignArgs A) {
         sp++;
     }
     // v = this lane's subtree root at height `sub`, index lane
-    for (int s = 0; s < 5; s++) {
+    for (int s = 0; s < g; s++) {
         const int hgt = sub + s;
         const uint32_t q = lane >> s;
         const bool holder = (lane & ((1u << s) - 1)) == 0;
-        if (holder && ((idx >> hgt) ^ 1u) == q) HF::store(sigt + N + (uint64_t)hgt * N, v);
+        if (valid && holder && ((idx >> hgt) ^ 1u) == q) HF::store(sigt + N + (uint64_t)hgt * N, v);
         uint32_t r[W];
 #pragma unroll
-        for (int x = 0; x < W; x++) r[x] = __shfl_down_sync(0xffffffffu, v[x], 1u << s);
+        for (int x = 0; x < W; x++) r[x] = __shfl_down_sync(0xffffffffu, v[x], 1u << s, G);
         if ((lane & ((2u << s) - 1)) == 0) {
             adrs_height(ad, hgt + 1);
             adrs_index(ad, (q >> 1) + (off >> (hgt + 1)));
             HF::H(v, v, r, ad, key);
         }
     }
-    if (lane == 0) HF::store(A.fors_roots + ((uint64_t)item * P.k + t) * N, v);
+    if (valid && lane == 0) HF::store(A.fors_roots + ((uint64_t)item * P.k + t) * N, v);
 }
 
 // ===========================================================================
@@ -340,6 +349,69 @@ struct TreeArgs {
     uint8_t *roots;         // [item][layer-layer0] n bytes
     uint8_t *sig;           // auth paths are written here when work != null
 };
+
+// Lane-per-tree variant for short subtrees: a thread reduces one whole
+// (item, layer) tree with a stack of hp+1 nodes; no shared memory, no idle
+// lanes in the upper levels.
+template <class HF>
+__global__ void k_trees_lane(SetParams P, TreeArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)A.count * A.nlayers) return;
+    const uint32_t item = (uint32_t)(gid / A.nlayers);
+    const int L = A.layer0 + (int)(gid % A.nlayers);
+    const uint32_t nleaf = 1u << P.hp;
+    const uint8_t *sk = A.sk.row(item);
+    KeyRegs<N> key;
+    uint64_t tree_L = 0;
+    uint32_t idx_L = 0;
+    if (A.work) {
+        const SignWork wk = A.work[item];
+        key_from_work<HF>(key, sk, sk + 2 * N, wk);
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    } else {
+        HF::key_init(key, sk, sk + 2 * N);
+    }
+    const uint8_t *lv = A.leaves + (((uint64_t)item * A.nlayers + (L - A.layer0)) * nleaf) * N;
+    uint8_t *auth = nullptr;
+    if (A.work)
+        auth = A.sig + (uint64_t)item * P.sig_bytes + N + P.fors_bytes +
+               (uint64_t)L * (P.wots_bytes + P.hp * N) + P.wots_bytes;
+    Adrs ad;
+    adrs_zero(ad);
+    adrs_layer(ad, L);
+    adrs_tree(ad, tree_L);
+    adrs_type(ad, ADDR_HASHTREE);
+    uint32_t stk[5][W];   // hp <= 4 in this variant
+    int heights[5];
+    int sp = 0;
+    for (uint32_t j = 0; j < nleaf; j++) {
+        uint32_t v[W];
+        HF::load(v, lv + (uint64_t)j * N);
+        if (auth && (idx_L ^ 1u) == j) HF::store(auth, v);
+        int hgt = 0;
+        while (sp > 0 && heights[sp - 1] == hgt) {
+            const uint32_t tidx = j >> (hgt + 1);
+            adrs_height(ad, hgt + 1);
+            adrs_index(ad, tidx);
+            uint32_t l[W];
+#pragma unroll
+            for (int x = 0; x < W; x++) l[x] = stk[sp - 1][x];
+            HF::H(v, l, v, ad, key);
+            sp--;
+            hgt++;
+            if (auth && hgt < P.hp && ((idx_L >> hgt) ^ 1u) == tidx) HF::store(auth + (uint64_t)hgt * N, v);
+        }
+#pragma unroll
+        for (int x = 0; x < W; x++) stk[sp][x] = v[x];
+        heights[sp] = hgt;
+        sp++;
+    }
+    uint32_t root[W];
+#pragma unroll
+    for (int x = 0; x < W; x++) root[x] = stk[0][x];
+    HF::store(A.roots + ((uint64_t)item * A.nlayers + (L - A.layer0)) * N, root);
+}
 
 template <class HF>
 __global__ void k_trees(SetParams P, TreeArgs A) {

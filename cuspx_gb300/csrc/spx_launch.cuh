@@ -18,6 +18,8 @@ struct Tuning {
     int tree_warps = 4;      // warps per block for k_trees (upper bound)
     int chains_per_warp = 64;  // (item, chain) tasks per warp in k_verify_chains
     int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers
+    int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
+    int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
 };
 
 struct KeygenArgs {
@@ -92,6 +94,11 @@ struct Family {
     }
 
     static void trees(const SetParams &P, const TreeArgs &T, const Tuning &tu, cudaStream_t s) {
+        if (tu.tree_mode == 1 && P.hp <= 4) {
+            const uint64_t threads = (uint64_t)T.count * T.nlayers;
+            k_trees_lane<HF><<<ceil_div(threads, 128), 128, 0, s>>>(P, T);
+            return;
+        }
         const uint64_t per_warp = 2ull * (1u << P.hp) * W * 4;
         int wpb = (int)(48 * 1024 / per_warp);
         if (wpb > tu.tree_warps) wpb = tu.tree_warps;
@@ -106,8 +113,9 @@ struct Family {
         CUSPX_MARK(pt, "k_sign_msg", s);
         {
             const int b = tu.fors_block;
-            const uint64_t threads = (uint64_t)A.count * P.k * 32;
-            k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - 4) * W * 4, s>>>(P, A);
+            const int g = tu.fors_lanes_log2 < P.a ? tu.fors_lanes_log2 : P.a;
+            const uint64_t threads = (((uint64_t)A.count * P.k) << g);
+            k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - g + 1) * W * 4, s>>>(P, A, g);
             CUSPX_MARK(pt, "k_fors_sign", s);
         }
         {

@@ -348,8 +348,33 @@ struct Sha2 {
         uint32_t hi = keep ? (0xffffffffu << (32 - 8 * keep)) : 0u;
         return (x & hi) | (0x80u << (24 - 8 * keep));
     }
+    // 16 big-endian message words starting at word q0, all inside m; the
+    // word offset keeps the alignment the prefix length gives (P % 4 == 0:
+    // 16-byte, P even: 8-byte, else 4-byte) since m itself is 16-byte aligned
+    template <int P>
+    SPX_DEV static void msg_block_full(uint32_t w[16], const uint8_t *m, uint64_t q0) {
+        const uint8_t *p = m + 4 * q0;
+        if (P % 4 == 0) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint4 v = reinterpret_cast<const uint4 *>(p)[i];
+                w[4 * i] = bswap32(v.x); w[4 * i + 1] = bswap32(v.y);
+                w[4 * i + 2] = bswap32(v.z); w[4 * i + 3] = bswap32(v.w);
+            }
+        } else if (P % 2 == 0) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const uint2 v = reinterpret_cast<const uint2 *>(p)[i];
+                w[2 * i] = bswap32(v.x); w[2 * i + 1] = bswap32(v.y);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; i++) w[i] = bswap32(reinterpret_cast<const uint32_t *>(p)[i]);
+        }
+    }
     // absorb prefix (P words, registers) || m into st, which has already
-    // absorbed pre_blocks 64-byte blocks; out = final state.
+    // absorbed pre_blocks 64-byte blocks; out = final state.  Blocks wholly
+    // inside the message are vector-loaded one block ahead of the compression.
     template <int P>
     SPX_DEV static void stream_msg(uint32_t st[8], uint32_t pre_blocks, const uint32_t pre[P], const uint8_t *m,
                                    uint64_t mlen) {
@@ -357,9 +382,15 @@ struct Sha2 {
         const uint64_t nblocks = (dbytes + 9 + 63) / 64;
         const uint64_t bits = (64 * (uint64_t)pre_blocks + dbytes) * 8;
         constexpr int PB = (P + 15) / 16;  // blocks that contain prefix words
+        auto full = [&](uint64_t b) { return b >= (uint64_t)PB && 4 * (16 * b - P + 16) <= mlen; };
+        uint32_t nxt[16];
+        bool have = false;
         for (uint64_t b = 0; b < nblocks; b++) {
             uint32_t w[16];
-            if (b < PB) {
+            if (have) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) w[j] = nxt[j];
+            } else if (b < PB) {
 #pragma unroll
                 for (int pb = 0; pb < PB; pb++) {
                     if (pb == (int)b) {
@@ -375,6 +406,8 @@ struct Sha2 {
 #pragma unroll
                 for (int j = 0; j < 16; j++) w[j] = msg_word(m, mlen, q0 + j);
             }
+            have = b + 1 < nblocks && full(b + 1);
+            if (have) msg_block_full<P>(nxt, m, 16 * (b + 1) - P);
             if (b == nblocks - 1) {
                 w[14] = (uint32_t)(bits >> 32);
                 w[15] = (uint32_t)bits;
@@ -619,16 +652,24 @@ struct Shake {
         uint64_t lo = keep ? (0xffffffffffffffffull >> (64 - 8 * keep)) : 0ull;
         return (x & lo) | (0x1Full << (8 * keep));
     }
-    // SHAKE256(prefix(P lanes) || m), squeezing up to 17 lanes into out
+    // SHAKE256(prefix(P lanes) || m) absorbed into A (state after the last
+    // permutation).  Blocks wholly inside the message are loaded one block
+    // ahead of the permutation (m + 8 * lane is 8-byte aligned).
     template <int P>
     SPX_DEV static void stream_msg(uint64_t A[25], const uint64_t pre[P], const uint8_t *m, uint64_t mlen) {
         const uint64_t dbytes = 8 * (uint64_t)P + mlen;
         const uint64_t nblocks = dbytes / 136 + 1;
         constexpr int PB = (P + 16) / 17;
+        auto full = [&](uint64_t b) { return b >= (uint64_t)PB && 8 * (17 * b - P + 17) <= mlen; };
+        uint64_t nxt[17];
+        bool have = false;
 #pragma unroll
         for (int i = 0; i < 25; i++) A[i] = 0;
         for (uint64_t b = 0; b < nblocks; b++) {
-            if (b < PB) {
+            if (have) {
+#pragma unroll
+                for (int j = 0; j < 17; j++) A[j] ^= nxt[j];
+            } else if (b < PB) {
 #pragma unroll
                 for (int pb = 0; pb < PB; pb++) {
                     if (pb == (int)b) {
@@ -643,6 +684,12 @@ struct Shake {
                 const uint64_t q0 = 17 * b - P;
 #pragma unroll
                 for (int j = 0; j < 17; j++) A[j] ^= msg_lane(m, mlen, q0 + j);
+            }
+            have = b + 1 < nblocks && full(b + 1);
+            if (have) {
+                const uint64_t *p = reinterpret_cast<const uint64_t *>(m + 8 * (17 * (b + 1) - P));
+#pragma unroll
+                for (int j = 0; j < 17; j++) nxt[j] = p[j];
             }
             // the 0x1F byte comes from msg_lane (the lane holding byte mlen is
             // always inside the last block); the final 0x80 is added here

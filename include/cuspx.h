@@ -67,8 +67,11 @@ typedef struct {
     int tree_warps;       /* warps per block, XMSS tree kernel */
     int chains_per_warp;  /* (item, chain) tasks per warp, verify chain kernel */
     int verify_mode;      /* 0 layered verify kernels, 1 one thread per item over all layers */
+    int fors_lanes_log2;  /* lanes per FORS tree = 2^g, g in 0..5 (0: lane per tree, 5: warp per tree) */
+    int tree_mode;        /* 0 warp per XMSS subtree, 1 lane per subtree (heights <= 4 only) */
 } cuspx_tuning;
-/* fields <= 0 (verify_mode < 0) keep the current value */
+/* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2
+ * and tree_mode, which keep it when < 0 */
 int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
 int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
 
@@ -132,6 +135,16 @@ int cuspx_batch_device_ptrs(cuspx_batch *b, void **keys, void **msgs, void **msg
  * the names and accumulated milliseconds (count entries). */
 int cuspx_batch_profile(cuspx_batch *b, int enable);
 int cuspx_batch_kernel_ms(cuspx_batch *b, int idx, const char **name, double *ms, long *launches);
+
+/* ---- mixed parameter sets in one launch ---------------------------------
+ * Runs the launch sequences of nb uploaded batches (any ops and sets of this
+ * context) as ONE CUDA graph: the graph forks onto every batch's stream so
+ * different parameter sets execute concurrently, and joins at the end.  The
+ * graph is captured on first use of a given (batches, counts, tunings)
+ * combination and replayed afterwards.  Synchronous; *ms (may be NULL)
+ * receives the device time of the whole graph.  Results are read with
+ * cuspx_batch_download on each batch. */
+int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *ms);
 
 /* ---- calibration --------------------------------------------------------
  * Measured integer-ALU peak of this GPU for the hash cores' instruction mix

@@ -158,3 +158,56 @@ def test_verify_mappings_agree(engine, setname):
             assert list(got) == want, (mode, cpw)
     finally:
         engine.set_tuning(sid, **saved)
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-simple", "sha256-128s-simple"])
+def test_sign_mappings_agree(engine, setname):
+    """Every sign launch mapping the autotuner may pick gives the same bytes."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(31)
+    seed = bytes(rng.randrange(256) for _ in range(3 * o.p.n))
+    pk, sk = o.seed_keypair(seed)
+    msgs = [bytes(rng.randrange(256) for _ in range(rng.randrange(0, 200))) for _ in range(5)]
+    want = [o.sign(m, sk) for m in msgs[:2]]
+    saved = engine.get_tuning(sid)
+    ref = None
+    try:
+        for g, tm, lb, fb in ((5, 0, 128, 128), (0, 1, 64, 64), (2, 1, 256, 96), (3, 0, 96, 256)):
+            engine.set_tuning(sid, fors_lanes_log2=g, tree_mode=tm, leaf_block=lb, fors_block=fb)
+            sigs, st = engine.sign_batch(sid, [sk] * len(msgs), msgs)
+            assert list(st) == [0] * len(msgs)
+            assert list(sigs[:2]) == want, (g, tm, lb, fb)
+            if ref is None:
+                ref = sigs
+            assert sigs == ref, (g, tm, lb, fb)
+    finally:
+        engine.set_tuning(sid, **saved)
+
+
+def test_mixed_sets_one_launch_vs_oracle(engine):
+    """Uneven lengths, distinct keys and two parameter sets in one graph launch
+    give the same signatures as the oracle item by item."""
+    import cuspx_gb300 as c
+    rng = random.Random(77)
+    names = ["sha256-128f-simple", "sha256-192f-robust", "shake256-128f-simple"]
+    oracles = {n: _oracle(n) for n in names}
+    keys = {}
+    for n in names:
+        o = oracles[n]
+        keys[n] = [o.seed_keypair(bytes(rng.randrange(256) for _ in range(3 * o.p.n))) for _ in range(3)]
+    set_ids, sks, msgs, expect = [], [], [], []
+    for i in range(24):
+        n = names[i % 3]
+        pk, sk = keys[n][rng.randrange(3)]
+        m = bytes(rng.randrange(256) for _ in range(int(2 ** rng.uniform(0, 12))))
+        set_ids.append(c.set_id(n)); sks.append(sk); msgs.append(m); expect.append((n, sk, m))
+    ms = c.MixedSigner(engine)
+    try:
+        for _ in range(2):   # captured on first use, replayed on the second
+            sigs, st, dev_ms = ms.sign(set_ids, sks, msgs)
+            assert list(st) == [0] * len(msgs) and dev_ms > 0
+        for (n, sk, m), sig in zip(expect, sigs):
+            assert sig == oracles[n].sign(m, sk), n
+    finally:
+        ms.close()

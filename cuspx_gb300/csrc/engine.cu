@@ -203,6 +203,18 @@ int cuspx_create(int device, cuspx_ctx **out) {
     if (e != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) return CUSPX_ECUDA;
     cuspx_ctx *c = new cuspx_ctx();
     c->device = device;
+    // default mappings by set shape (what the autotuner settled on for the
+    // reference sets on GB300): one lane per FORS tree for short FORS trees,
+    // a lane per XMSS subtree for subtrees of height <= 4, 256-thread leaf
+    // blocks where registers allow it (SHA-256 simple)
+    for (int i = 0; i < kNumSets; i++) {
+        const SetDesc &sd = kSets[i];
+        Tuning &t = c->tune[i];
+        t.fors_lanes_log2 = sd.a <= 8 ? 0 : std::min(5, sd.a - 6);
+        t.tree_mode = sd.h / sd.d <= 4 ? 1 : 0;
+        t.leaf_block = (sd.hash == 0 && !sd.robust) ? 256 : 128;
+        t.chains_per_warp = sd.hash == 1 ? 256 : 128;
+    }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;
         return CUSPX_ECUDA;

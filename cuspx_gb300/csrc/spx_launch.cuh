@@ -113,7 +113,10 @@ struct Family {
         CUSPX_MARK(pt, "k_sign_msg", s);
         {
             const int b = tu.fors_block;
-            const int g = tu.fors_lanes_log2 < P.a ? tu.fors_lanes_log2 : P.a;
+            // small batches: spread each tree over more lanes until the launch
+            // has about one full wave of threads (152 SMs x 128), for latency
+            int g = tu.fors_lanes_log2 < P.a ? tu.fors_lanes_log2 : P.a;
+            while (g < 5 && g < P.a && (((uint64_t)A.count * P.k) << g) < 152ull * 128) g++;
             const uint64_t threads = (((uint64_t)A.count * P.k) << g);
             k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - g + 1) * W * 4, s>>>(P, A, g);
             CUSPX_MARK(pt, "k_fors_sign", s);

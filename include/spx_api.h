@@ -50,6 +50,54 @@ int crypto_sign_open(unsigned char *m, unsigned long long *mlen, const unsigned 
 void randombytes_init(unsigned char *entropy_input, unsigned char *personalization_string, int security_strength);
 int randombytes(unsigned char *x, unsigned long long xlen);
 
+/*
+ * The reference's GPU faces (api.h:49-176), same names and buffer layouts.
+ * The variants differ in the reference only by their parallel scheme ("ap"
+ * algorithmic, "dp/mdp/sdp" thread per signature, "mhp" hybrid with
+ * intra_para threads, "ms" multi-stream, "mgpu" two devices); here every
+ * variant is the same batched GPU engine with the autotuned mapping, so
+ * intra_para is accepted and ignored.  Unlike the reference they compute
+ * exactly the CPU path's bytes (optrand 0xAD..., sign.cu:1951-1954) and
+ * verify every item (the reference's batched open reports task 0 only).
+ *   single:  face_crypto_sign_keypair / face_crypto_sign / face_crypto_sign_open
+ *            (and the face_ap_* aliases)
+ *   batched: sk/pk are num rows; m is num messages of mlen bytes each; sm is
+ *            num rows of (sig || m_i), smlen the length of one row; open
+ *            writes num messages of smlen - CRYPTO_BYTES bytes into m,
+ *            zero-filling the rows that fail, and returns 0 only if every
+ *            item verified (else -1).
+ */
+int face_crypto_sign_keypair(unsigned char *pk, unsigned char *sk);
+int face_ap_crypto_sign_keypair(unsigned char *pk, unsigned char *sk);
+int face_crypto_sign(unsigned char *sm, unsigned long long *smlen, const unsigned char *m, unsigned long long mlen,
+                     const unsigned char *sk);
+int face_ap_crypto_sign(unsigned char *sm, unsigned long long *smlen, const unsigned char *m,
+                        unsigned long long mlen, const unsigned char *sk);
+int face_crypto_sign_open(unsigned char *m, unsigned long long *mlen, const unsigned char *sm,
+                          unsigned long long smlen, const unsigned char *pk);
+int face_ap_crypto_sign_open(unsigned char *m, unsigned long long *mlen, const unsigned char *sm,
+                             unsigned long long smlen, const unsigned char *pk);
+int face_mdp_crypto_sign_keypair(unsigned char *pk, unsigned char *sk, unsigned int num);
+int face_mhp_crypto_sign_keypair(unsigned char *pk, unsigned char *sk, unsigned int num, unsigned int intra_para);
+int face_mhp_crypto_sign_keypair_scheme2(unsigned char *pk, unsigned char *sk, unsigned int num,
+                                         unsigned int intra_para);
+int face_mdp_crypto_sign(unsigned char *sm, unsigned long long *smlen, const unsigned char *m,
+                         unsigned long long mlen, const unsigned char *sk, unsigned int dp_num);
+int face_sdp_crypto_sign(unsigned char *sm, unsigned long long *smlen, const unsigned char *m,
+                         unsigned long long mlen, const unsigned char *sk, unsigned int dp_num);
+int face_mhp_crypto_sign(unsigned char *sm, unsigned long long *smlen, const unsigned char *m,
+                         unsigned long long mlen, const unsigned char *sk, unsigned int dp_num);
+int face_mhp_crypto_sign_scheme2(unsigned char *sm, unsigned long long *smlen, const unsigned char *m,
+                                 unsigned long long mlen, const unsigned char *sk, unsigned int dp_num,
+                                 unsigned int intra_para);
+int face_mdp_crypto_sign_open(unsigned char *m, unsigned long long *mlen, const unsigned char *sm,
+                              unsigned long long smlen, const unsigned char *pk, unsigned int dp_num);
+int face_sdp_crypto_sign_open(unsigned char *m, unsigned long long *mlen, const unsigned char *sm,
+                              unsigned long long smlen, const unsigned char *pk, unsigned int dp_num);
+int face_mhp_crypto_sign_open(unsigned char *m, unsigned long long *mlen, const unsigned char *sm,
+                              unsigned long long smlen, const unsigned char *pk, unsigned int dp_num,
+                              unsigned int intra_para);
+
 #ifdef __cplusplus
 }
 #endif

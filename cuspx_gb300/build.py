@@ -81,7 +81,7 @@ def build(verbose=False, jobs=None, ptxas_verbose=False):
                 cmd = [nvcc] + NVCC_FLAGS + extra + [f"-DFAMILY_HASH={h}", f"-DFAMILY_N={n}", f"-DFAMILY_ROBUST={r}",
                                                      "-c", fam_src, "-o", obj]
                 steps.append((obj, [fam_src] + headers, cmd))
-    for src in ("engine.cu", "serve.cu", "calib.cu"):
+    for src in ("engine.cu", "serve.cu", "calib.cu", "noalloc.cu"):
         s = os.path.join(CSRC, src)
         if os.path.exists(s):
             obj = os.path.join(BUILD, src.replace(".cu", ".o"))

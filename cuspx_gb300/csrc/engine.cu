@@ -69,6 +69,9 @@ static const FamilyOps &family_of(int set) {
     const SetDesc &s = kSets[set];
     return g_family[s.hash][s.n / 8 - 2][s.robust];
 }
+
+// registration for other translation units of the library
+void ensure_registered() { register_all(); }
 }  // namespace cuspx
 
 using namespace cuspx;

@@ -37,6 +37,7 @@ extern "C" {
 #define CUSPX_ENOMEM (-3)     /* device memory budget exceeded */
 #define CUSPX_EBUSY (-4)      /* queue full / would exceed admission budget */
 #define CUSPX_ETIMEDOUT (-5)  /* wait expired */
+#define CUSPX_ETOOBIG (-6)    /* request larger than the fixed no-allocation scratch */
 
 enum { CUSPX_OP_KEYGEN = 0, CUSPX_OP_SIGN = 1, CUSPX_OP_VERIFY = 2 };
 
@@ -145,6 +146,34 @@ int cuspx_batch_kernel_ms(cuspx_batch *b, int idx, const char **name, double *ms
  * receives the device time of the whole graph.  Results are read with
  * cuspx_batch_download on each batch. */
 int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *ms);
+
+/* ---- signing without device allocation ----------------------------------
+ * No counterpart in the reference (whose GPU faces cudaMalloc and cudaFree on
+ * every call).  For callers that must not allocate device memory while they
+ * run: cudaFree waits for the whole device and stalls every other stream,
+ * and hosts that own all device memory through their own allocator forbid a
+ * library from allocating.  The caller passes DEVICE pointers for all inputs
+ * and outputs (same layouts as cuspx_sign_batch: count sk rows of 4n bytes;
+ * a message slab with 16-byte aligned offsets, readable up to the next
+ * multiple of 16 past each message; optrand count x n or NULL for the
+ * reference's 0xAD bytes; count x sig_bytes signatures; count statuses) and
+ * the cudaStream_t to run on (NULL: legacy default stream).  The call is
+ * asynchronous on that stream and allocates nothing: its scratch is an
+ * 8 MiB array in the library's device image, held by every GPU that loads
+ * the library until the process exits.
+ *   - Limit: count must fit the 8 MiB scratch; the per-signature need is
+ *     d*len*16*n + d*2^h'*n + d*n + k*n + 96 bytes (about 196 KiB at 128f:
+ *     41 signatures; 118 KiB at 128s: 69; 426 KiB at 192f: 19; 580 KiB at
+ *     256f: 14).  Larger batches return CUSPX_ETOOBIG and launch nothing.
+ *   - The first call on a device (with that device current) resolves the
+ *     array's device address and configures the kernels; make that first
+ *     call before any stream capture.
+ *   - Every call shares the array: calls that overlap on the GPU race and
+ *     must be serialised by the caller.  It is never cleared; no scratch
+ *     value is read before the same call writes it. */
+int cuspx_sign_noalloc(int set, size_t count, const uint8_t *d_sks, const uint8_t *d_msgs,
+                       const uint64_t *d_msg_off, const uint64_t *d_msg_len, const uint8_t *d_optrand,
+                       uint8_t *d_sigs, int32_t *d_status, void *stream);
 
 /* ---- calibration --------------------------------------------------------
  * Measured integer-ALU peak of this GPU for the hash cores' instruction mix

@@ -416,9 +416,14 @@ def served_runs(c, eng, seconds=2.0):
     for rate in (5e3, 20e3, 50e3, 100e3, 200e3):
         r = srv.loadgen(rate, seconds, sids, per, verify_frac=0.7, min_len=16, max_len=1 << 20, corrupt_frac=0.0,
                         seed=7 + int(rate), pool=48)
+        ms = lambda v: [round(x / 1e3, 3) for x in v]
         pts.append({"rate": rate, "sign_per_s": r["sign_throughput"], "verify_per_s": r["verify_throughput"],
                     "sign_p50_ms": r["sign_p50_us"] / 1e3, "sign_p99_ms": r["sign_p99_us"] / 1e3,
                     "verify_p50_ms": r["verify_p50_us"] / 1e3, "verify_p99_ms": r["verify_p99_us"] / 1e3,
+                    "by_length_le1KiB_le64KiB_gt64KiB": {
+                        "sign_p50_ms": ms(r["sign_p50_bucket_us"]), "sign_p99_ms": ms(r["sign_p99_bucket_us"]),
+                        "verify_p50_ms": ms(r["verify_p50_bucket_us"]),
+                        "verify_p99_ms": ms(r["verify_p99_bucket_us"])},
                     "completed": r["completed"], "refused": r["refused"], "wrong_verdicts": r["wrong_verdicts"],
                     "mean_batch": r["mean_batch"]})
     srv.close()

@@ -358,10 +358,21 @@ class ServeCounters(ctypes.Structure):
                                                  "sign_done", "verify_done")] + \
                [("bytes_inflight", ctypes.c_size_t), ("bytes_peak", ctypes.c_size_t)] + \
                [(f, ctypes.c_double) for f in ("sign_p50_us", "sign_p99_us", "verify_p50_us", "verify_p99_us",
-                                                 "mean_batch")]
+                                                 "mean_batch")] + \
+               [(f, ctypes.c_double * 3) for f in ("sign_p50_bucket_us", "sign_p99_bucket_us",
+                                                     "verify_p50_bucket_us", "verify_p99_bucket_us")] + \
+               [("bucket_count", (ctypes.c_uint64 * 3) * 2)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        out = {}
+        for f, _ in self._fields_:
+            v = getattr(self, f)
+            if f == "bucket_count":
+                v = [list(v[0]), list(v[1])]
+            elif isinstance(v, ctypes.Array):
+                v = list(v)
+            out[f] = v
+        return out
 
 
 class LoadgenConfig(ctypes.Structure):
@@ -376,10 +387,13 @@ class LoadgenResult(ctypes.Structure):
                                                  "verify_done")] + \
                [(f, ctypes.c_double) for f in ("wall_s", "throughput", "sign_throughput", "verify_throughput",
                                                  "sign_p50_us", "sign_p99_us", "verify_p50_us", "verify_p99_us",
-                                                 "mean_batch")]
+                                                 "mean_batch")] + \
+               [(f, ctypes.c_double * 3) for f in ("sign_p50_bucket_us", "sign_p99_bucket_us",
+                                                     "verify_p50_bucket_us", "verify_p99_bucket_us")]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        return {f: (list(getattr(self, f)) if isinstance(getattr(self, f), ctypes.Array) else getattr(self, f))
+                for f, _ in self._fields_}
 
 
 SERVE_EXPORTS = ["cuspx_serve_create", "cuspx_serve_destroy", "cuspx_serve_add_keys", "cuspx_serve_add_pubkeys",

@@ -73,8 +73,14 @@ struct Slot {
     std::vector<Req *> reqs;
 };
 
+// Requests are grouped per (operation, set, length class): messages longer
+// than kLongMsg take milliseconds of serial hashing on one thread, so they
+// are launched in batches of their own that run beside the short ones
+// instead of holding every short request of a shared batch back.
+constexpr size_t kLongMsg = 16384;
+
 struct Group {
-    int op = 0, set = 0;
+    int op = 0, set = 0, long_class = 0;
     std::deque<Req *> pending;
     std::vector<Slot *> slots;
     size_t per_item = 0;
@@ -99,15 +105,18 @@ struct cuspx_server {
     std::thread th;
     bool stop = false;
     std::vector<KeyTable> keys;
-    std::vector<Group> groups;   // index (op - 1) * kNumSets + set
+    std::vector<Group> groups;   // index ((op - 1) * kNumSets + set) * 2 + long_class
     std::unordered_map<uint64_t, Req *> live;
     uint64_t next_ticket = 1;
     size_t pending_total = 0, bytes_inflight = 0, bytes_peak = 0, bytes_alloc = 0;
     uint64_t submitted = 0, completed = 0, refused = 0, failed = 0, launches = 0, batched = 0;
     uint64_t sign_done = 0, verify_done = 0, wrong = 0;
     std::vector<float> lat_sign, lat_verify;
+    std::vector<float> lat_bucket[2][3];   // [sign, verify][<= 1 KiB, <= 64 KiB, > 64 KiB]
     Clock::time_point last_done;
 };
+
+static int len_bucket(size_t mlen) { return mlen <= 1024 ? 0 : (mlen <= 65536 ? 1 : 2); }
 
 static size_t item_bytes(int op, const SetParams &P) {
     const size_t n = P.n;
@@ -217,6 +226,7 @@ static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
             s->lat_verify.push_back(us);
             s->verify_done++;
         }
+        s->lat_bucket[g.op == CUSPX_OP_SIGN ? 0 : 1][len_bucket(r->mlen)].push_back(us);
         if (r->expect != 1 && r->status != r->expect) s->wrong++;
         s->completed++;
         if (r->flags & CUSPX_SUBMIT_DETACH) {
@@ -328,15 +338,17 @@ int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_serv
     if (!s->cfg.max_queue) s->cfg.max_queue = 1u << 20;
     cudaGetDevice(&s->device);
     s->keys.resize(kNumSets);
-    s->groups.resize(2 * kNumSets);
+    s->groups.resize(4 * kNumSets);
     for (int op = 1; op <= 2; op++)
-        for (int set = 0; set < kNumSets; set++) {
-            Group &g = s->groups[(op - 1) * kNumSets + set];
-            g.op = op;
-            g.set = set;
-            g.P = make_params(kSets[set]);
-            g.per_item = item_bytes(op, g.P);
-        }
+        for (int set = 0; set < kNumSets; set++)
+            for (int lc = 0; lc < 2; lc++) {
+                Group &g = s->groups[((op - 1) * kNumSets + set) * 2 + lc];
+                g.op = op;
+                g.set = set;
+                g.long_class = lc;
+                g.P = make_params(kSets[set]);
+                g.per_item = item_bytes(op, g.P);
+            }
     s->th = std::thread(scheduler, s);
     *out = s;
     return CUSPX_OK;
@@ -428,7 +440,7 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     r->siglen = op == CUSPX_OP_VERIFY ? siglen : 0;
     std::unique_lock<std::mutex> lk(s->mu);
     const KeyTable &kt = s->keys[set];
-    Group &g = s->groups[(op - 1) * kNumSets + set];
+    Group &g = s->groups[((op - 1) * kNumSets + set) * 2 + (mlen > kLongMsg ? 1 : 0)];
     int rc = CUSPX_OK;
     if (s->stop) rc = CUSPX_EBUSY;
     else if (key_id >= kt.n || (op == CUSPX_OP_SIGN && !kt.has_sk[key_id])) rc = CUSPX_EINVAL;
@@ -478,9 +490,11 @@ int cuspx_serve_wait(cuspx_server *s, uint64_t ticket, long timeout_us, uint8_t 
 
 int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st) {
     if (!s || !st) return CUSPX_EINVAL;
-    std::vector<float> ls, lv;
+    std::vector<float> ls, lv, lb[2][3];
     {
         std::lock_guard<std::mutex> lk(s->mu);
+        for (int o = 0; o < 2; o++)
+            for (int b = 0; b < 3; b++) lb[o][b] = s->lat_bucket[o][b];
         st->submitted = s->submitted;
         st->completed = s->completed;
         st->refused = s->refused;
@@ -498,6 +512,14 @@ int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st) {
     st->sign_p99_us = percentile(ls, 0.99);
     st->verify_p50_us = percentile(lv, 0.50);
     st->verify_p99_us = percentile(lv, 0.99);
+    for (int b = 0; b < 3; b++) {
+        st->sign_p50_bucket_us[b] = percentile(lb[0][b], 0.50);
+        st->sign_p99_bucket_us[b] = percentile(lb[0][b], 0.99);
+        st->verify_p50_bucket_us[b] = percentile(lb[1][b], 0.50);
+        st->verify_p99_bucket_us[b] = percentile(lb[1][b], 0.99);
+        st->bucket_count[0][b] = lb[0][b].size();
+        st->bucket_count[1][b] = lb[1][b].size();
+    }
     return CUSPX_OK;
 }
 
@@ -509,6 +531,8 @@ int cuspx_serve_reset_stats(cuspx_server *s) {
     s->bytes_peak = s->bytes_inflight;
     s->lat_sign.clear();
     s->lat_verify.clear();
+    for (auto &o : s->lat_bucket)
+        for (auto &b : o) b.clear();
     return CUSPX_OK;
 }
 
@@ -630,6 +654,12 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
     out->verify_p50_us = st.verify_p50_us;
     out->verify_p99_us = st.verify_p99_us;
     out->mean_batch = st.mean_batch;
+    for (int b = 0; b < 3; b++) {
+        out->sign_p50_bucket_us[b] = st.sign_p50_bucket_us[b];
+        out->sign_p99_bucket_us[b] = st.sign_p99_bucket_us[b];
+        out->verify_p50_bucket_us[b] = st.verify_p50_bucket_us[b];
+        out->verify_p99_bucket_us[b] = st.verify_p99_bucket_us[b];
+    }
     return st.completed + refused == offered ? CUSPX_OK : CUSPX_ETIMEDOUT;
 }
 

@@ -279,7 +279,7 @@ struct LeafArgs {
 };
 
 template <class HF>
-__global__ void k_leaves(SetParams P, LeafArgs A) {
+__global__ void __launch_bounds__(256, HF::kLeafMinBlocks) k_leaves(SetParams P, LeafArgs A) {
     constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
     extern __shared__ uint32_t smem[];
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -17,6 +17,10 @@
 #pragma once
 #include "spx_hash.cuh"
 
+#ifndef CUSPX_ROBUST_LEAF_MINBLOCKS
+#define CUSPX_ROBUST_LEAF_MINBLOCKS 2
+#endif
+
 namespace cuspx {
 
 // Per-item key material in registers.  mid is the SHA-256 state after the
@@ -69,6 +73,9 @@ struct Sha2 {
     static constexpr int W = N / 4;
     static constexpr bool kRobust = ROBUST;
     static constexpr int kShake = 0;
+    // k_leaves register budget: robust chains carry a second (mask) state and
+    // would otherwise leave only 2-3 blocks per SM
+    static constexpr int kLeafMinBlocks = ROBUST ? CUSPX_ROBUST_LEAF_MINBLOCKS : 1;
 
     // memory <-> register order
     SPX_DEV static void load(uint32_t v[W], const uint8_t *p) {
@@ -481,6 +488,7 @@ struct Shake {
     static constexpr int NL = N / 8;  // lanes per value
     static constexpr bool kRobust = ROBUST;
     static constexpr int kShake = 1;
+    static constexpr int kLeafMinBlocks = 1;
 
     SPX_DEV static void load(uint32_t v[W], const uint8_t *p) { load_bytes_le<N>(v, p); }
     SPX_DEV static void store(uint8_t *p, const uint32_t v[W]) { store_bytes_le<N>(p, v); }

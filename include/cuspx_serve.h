@@ -14,7 +14,10 @@
  *   - a launch is admitted only while the device bytes of all in-flight
  *     launches stay within `mem_budget`; submissions beyond `max_queue`
  *     pending requests are refused with CUSPX_EBUSY;
- *   - per-request latency (submit to result on the host) feeds p50/p99.
+ *   - requests with messages over 16 KiB are batched apart from shorter ones
+ *     (their serial message hashing would hold a shared batch back);
+ *   - per-request latency (submit to result on the host) feeds p50/p99,
+ *     overall and per message-length bucket.
  * Results of a request do not depend on what it was batched with.
  */
 #ifndef CUSPX_SERVE_H
@@ -46,6 +49,9 @@ typedef struct {
     size_t bytes_inflight, bytes_peak;
     double sign_p50_us, sign_p99_us, verify_p50_us, verify_p99_us;
     double mean_batch;
+    /* latency by message length: [0] <= 1 KiB, [1] <= 64 KiB, [2] > 64 KiB */
+    double sign_p50_bucket_us[3], sign_p99_bucket_us[3], verify_p50_bucket_us[3], verify_p99_bucket_us[3];
+    uint64_t bucket_count[2][3];   /* [sign, verify][bucket] */
 } cuspx_serve_counters;
 
 /* submit flags */
@@ -91,6 +97,7 @@ typedef struct {
     double wall_s, throughput, sign_throughput, verify_throughput;
     double sign_p50_us, sign_p99_us, verify_p50_us, verify_p99_us;
     double mean_batch;
+    double sign_p50_bucket_us[3], sign_p99_bucket_us[3], verify_p50_bucket_us[3], verify_p99_bucket_us[3];
 } cuspx_loadgen_result;
 
 int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *cfg, cuspx_loadgen_result *out);

@@ -32,7 +32,7 @@ build_one() {
     case "$hash" in sha256) hdef=SHA256;; shake256) hdef=SHAKE256;; *) echo "bad set $set" >&2; return 2;; esac
     sdef="SPX_$(echo "$size" | tr a-z A-Z)"
     dir="$OUT/$set"
-    if [ -x "$dir/ref_golden" ] && [ "$dir/ref_golden" -nt "$HERE/ref_golden.cu" ]; then return 0; fi
+    if [ -x "$dir/ref_golden" ] && [ -x "$dir/PQCgenKAT_sign" ] && [ "$dir/ref_golden" -nt "$HERE/ref_golden.cu" ]; then return 0; fi
     mkdir -p "$dir"
     local flags="-ccbin g++ --expt-relaxed-constexpr -O3 -m64 -dc -arch=$ARCH -w -I$HERE/shim -I$REF -DVARIANT -D$hdef -D$sdef -DSIMPLE"
     local objs=""
@@ -41,8 +41,11 @@ build_one() {
         objs="$objs $dir/${s%.cu}.o"
     done
     nvcc $flags -o "$dir/ref_golden.o" "$HERE/ref_golden.cu" &
+    nvcc $flags -o "$dir/PQCgenKAT_sign.o" "$REF/PQCgenKAT_sign.cu" &
     wait
     nvcc -arch=$ARCH -o "$dir/ref_golden" $objs "$dir/ref_golden.o" -Xlinker "$LIBCRYPTO" -lstdc++ -lm
+    # the reference's own NIST KAT generator (PQCgenKAT_sign.cu), same objects
+    nvcc -arch=$ARCH -o "$dir/PQCgenKAT_sign" $objs "$dir/PQCgenKAT_sign.o" -Xlinker "$LIBCRYPTO" -lstdc++ -lm
 }
 
 for s in $SETS; do build_one "$s"; done

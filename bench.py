@@ -29,6 +29,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# many concurrent streams (serving, mixed-set graphs): 32 hardware queues,
+# set before anything creates the CUDA context
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 SET = "sha256-128f-simple"
 BATCH = 4096
@@ -425,7 +428,8 @@ def served_runs(c, eng, seconds=2.0):
                         "verify_p50_ms": ms(r["verify_p50_bucket_us"]),
                         "verify_p99_ms": ms(r["verify_p99_bucket_us"])},
                     "completed": r["completed"], "refused": r["refused"], "wrong_verdicts": r["wrong_verdicts"],
-                    "mean_batch": r["mean_batch"]})
+                    "mean_batch": r["mean_batch"], "launch_ms_mean": r["launch_ms_mean"],
+                    "launch_ms_max": r["launch_ms_max"]})
     srv.close()
     out["served_stream"] = {"sets": names, "keys": per * len(sids), "lengths": "log-uniform 16 B..1 MiB",
                             "points": pts}

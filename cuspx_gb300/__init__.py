@@ -38,7 +38,8 @@ class CuspxError(RuntimeError):
 class Tuning(ctypes.Structure):
     """cuspx_tuning: the launch mapping of one parameter set."""
     _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
-                                            "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode")]
+                                            "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode",
+                                            "chain_mode_max")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -188,7 +189,7 @@ class Engine:
 
     def set_tuning(self, sid, **kw):
         """Change fields of a set's launch mapping (others keep their value)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")
@@ -361,7 +362,8 @@ class ServeCounters(ctypes.Structure):
                                                  "mean_batch")] + \
                [(f, ctypes.c_double * 3) for f in ("sign_p50_bucket_us", "sign_p99_bucket_us",
                                                      "verify_p50_bucket_us", "verify_p99_bucket_us")] + \
-               [("bucket_count", (ctypes.c_uint64 * 3) * 2)]
+               [("bucket_count", (ctypes.c_uint64 * 3) * 2)] + \
+               [("launch_ms_mean", ctypes.c_double), ("launch_ms_max", ctypes.c_double)]
 
     def as_dict(self):
         out = {}
@@ -389,7 +391,8 @@ class LoadgenResult(ctypes.Structure):
                                                  "sign_p50_us", "sign_p99_us", "verify_p50_us", "verify_p99_us",
                                                  "mean_batch")] + \
                [(f, ctypes.c_double * 3) for f in ("sign_p50_bucket_us", "sign_p99_bucket_us",
-                                                     "verify_p50_bucket_us", "verify_p99_bucket_us")]
+                                                     "verify_p50_bucket_us", "verify_p99_bucket_us")] + \
+               [("launch_ms_mean", ctypes.c_double), ("launch_ms_max", ctypes.c_double)]
 
     def as_dict(self):
         return {f: (list(getattr(self, f)) if isinstance(getattr(self, f), ctypes.Array) else getattr(self, f))

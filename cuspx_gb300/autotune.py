@@ -5,8 +5,9 @@ HP_PARALLELISM, block-size and load-balancing switches).  Here the mapping is
 a runtime cuspx_tuning per parameter set, and this module picks it by timing
 real batches on the device:
 
-  sign:   fors_lanes_log2 (lanes per FORS tree), tree_mode, leaf_block,
-          fors_block, tree_warps
+  sign:   chain_mode_max (lane per chain vs lane per leaf for this batch
+          size), fors_lanes_log2 (lanes per FORS tree), tree_mode,
+          leaf_block, fors_block, tree_warps
   verify: chains_per_warp, verify_block, verify_mode
 
 Search is coordinate descent: each knob is swept with the others held, the
@@ -23,6 +24,7 @@ import numpy as np
 from . import OP_SIGN, OP_VERIFY, pack_messages, set_name, set_sizes
 
 SIGN_SPACE = {
+    "chain_mode_max": [0, 256],
     "fors_lanes_log2": [0, 1, 2, 3, 5],
     "tree_mode": [0, 1],
     "leaf_block": [64, 128, 256],

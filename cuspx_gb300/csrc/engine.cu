@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -76,6 +77,10 @@ void ensure_registered() { register_all(); }
 
 using namespace cuspx;
 
+// items per batch for which chain-parallel leaf scratch is allocated (the
+// largest chain_mode_max that can take effect)
+static const size_t kChainModeItems = 256;
+
 struct cuspx_ctx {
     int device = 0;
     std::string err;
@@ -120,6 +125,8 @@ struct cuspx_batch {
     SignWork *work = nullptr;
     uint8_t *fors_roots = nullptr, *leaves = nullptr, *roots = nullptr, *chains = nullptr;
     uint8_t *wpk = nullptr, *cur_root = nullptr;
+    uint8_t *ends = nullptr;   // chain-parallel leaf scratch
+    uint32_t ends_cap = 0;
     size_t count = 0;
     bool use_keyrow = false, use_aux = false, use_siglen = false;
     const uint8_t *bound_keys = nullptr;   // external device key table (not owned)
@@ -200,6 +207,11 @@ int cuspx_set_sizes(int set, size_t *pk, size_t *sk, size_t *sig, size_t *seed, 
 int cuspx_create(int device, cuspx_ctx **out) {
     if (!out) return CUSPX_EINVAL;
     *out = nullptr;
+    // Concurrent batches and serving launches use many streams; with the
+    // default 8 hardware work queues, streams share queues and a short launch
+    // can wait behind a long kernel of another stream.  Ask for 32 (read when
+    // the process creates its CUDA context; a caller's own setting is kept).
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     register_all();
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -279,6 +291,7 @@ int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
         if (in->tree_mode > 1) return fail(ctx, CUSPX_EINVAL, "tree_mode must be 0 or 1");
         t.tree_mode = in->tree_mode;
     }
+    if (in->chain_mode_max >= 0) t.chain_mode_max = in->chain_mode_max;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->tune[set] = t;   // batches re-capture their graph when the mapping changed
     return CUSPX_OK;
@@ -295,6 +308,7 @@ int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
     out->verify_mode = t.verify_mode;
     out->fors_lanes_log2 = t.fors_lanes_log2;
     out->tree_mode = t.tree_mode;
+    out->chain_mode_max = t.chain_mode_max;
     return CUSPX_OK;
 }
 
@@ -356,6 +370,9 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
         A((void **)&b->out, cap * 2 * n);
         A((void **)&b->leaves, cap * ((size_t)1 << P.hp) * n);
         A((void **)&b->roots, cap * n);
+        // chain-parallel scratch for small key batches
+        b->ends_cap = (uint32_t)std::min<size_t>(cap, (size_t)kChainModeItems * P.d);
+        A((void **)&b->ends, (size_t)b->ends_cap * ((size_t)1 << P.hp) * P.len * n);
     } else {
         A((void **)&b->keyrow, cap * sizeof(uint32_t));
         A((void **)&b->msg, msg_capacity + 64);
@@ -369,6 +386,9 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
             A((void **)&b->leaves, cap * P.d * ((size_t)1 << P.hp) * n);
             A((void **)&b->roots, cap * P.d * n);
             A((void **)&b->chains, cap * P.d * P.len * 16 * n);
+            // chain-parallel scratch for small batches
+            b->ends_cap = (uint32_t)std::min<size_t>(cap, kChainModeItems);
+            A((void **)&b->ends, (size_t)b->ends_cap * P.d * ((size_t)1 << P.hp) * P.len * n);
         } else {
             A((void **)&b->aux, cap * P.sig_bytes);
             A((void **)&b->siglen, cap * sizeof(uint64_t));
@@ -474,6 +494,8 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.roots = b->roots;
         A.chains = b->chains;
         A.status = b->status;
+        A.ends = b->ends;
+        A.ends_cap = b->ends_cap;
         ops.sign(P, A, tu, b->s, pt);
     } else if (b->op == CUSPX_OP_VERIFY) {
         VerifyArgs A;
@@ -491,7 +513,7 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.cur_root = b->cur_root;
         ops.verify(P, A, tu, b->s, pt);
     } else {
-        KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots};
+        KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots, b->ends, b->ends_cap};
         ops.keygen(P, K, tu, b->s, pt);
     }
 }
@@ -618,6 +640,26 @@ int cuspx_batch_last_ms(cuspx_batch *b, float *ms) {
 }
 
 void *cuspx_batch_stream(cuspx_batch *b) { return b ? (void *)b->s : nullptr; }
+
+}  // extern "C"
+
+namespace cuspx {
+// Library-internal: give an idle batch a stream of the given priority (lower
+// numbers run first); its captured graphs are dropped with the old stream.
+int batch_set_stream_priority(cuspx_batch *b, int priority) {
+    if (!b) return CUSPX_EINVAL;
+    CK(cudaStreamSynchronize(b->s), b->ctx);
+    cudaStream_t ns;
+    CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, priority), b->ctx);
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
+    b->graphs.clear();
+    cudaStreamDestroy(b->s);
+    b->s = ns;
+    return CUSPX_OK;
+}
+}  // namespace cuspx
+
+extern "C" {
 
 int cuspx_batch_bind_keys(cuspx_batch *b, const void *d_keys, size_t nkeys) {
     if (!b || b->op == CUSPX_OP_KEYGEN) return CUSPX_EINVAL;

@@ -29,6 +29,7 @@
 
 namespace cuspx {
 SetParams make_params(const SetDesc &s);
+int batch_set_stream_priority(cuspx_batch *b, int priority);
 }
 using namespace cuspx;
 using Clock = std::chrono::steady_clock;
@@ -68,6 +69,7 @@ struct Slot {
     uint8_t *h_aux = nullptr, *h_out = nullptr;
     int32_t *h_status = nullptr;
     cudaEvent_t ev = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_end = nullptr;   // device time of the launch
     bool busy = false;
     size_t bytes = 0;
     std::vector<Req *> reqs;
@@ -78,6 +80,10 @@ struct Slot {
 // are launched in batches of their own that run beside the short ones
 // instead of holding every short request of a shared batch back.
 constexpr size_t kLongMsg = 16384;
+// Message area of one launch: a full batch of short messages, or 64 MiB of
+// long ones.  Slots are created once at this size and never re-created
+// (freeing device or pinned memory waits for the whole device).
+constexpr size_t kLongLaunchBytes = (size_t)64 << 20;
 
 struct Group {
     int op = 0, set = 0, long_class = 0;
@@ -111,6 +117,7 @@ struct cuspx_server {
     size_t pending_total = 0, bytes_inflight = 0, bytes_peak = 0, bytes_alloc = 0;
     uint64_t submitted = 0, completed = 0, refused = 0, failed = 0, launches = 0, batched = 0;
     uint64_t sign_done = 0, verify_done = 0, wrong = 0;
+    double launch_ms_sum = 0, launch_ms_max = 0;
     std::vector<float> lat_sign, lat_verify;
     std::vector<float> lat_bucket[2][3];   // [sign, verify][<= 1 KiB, <= 64 KiB, > 64 KiB]
     Clock::time_point last_done;
@@ -139,34 +146,39 @@ static void free_slot(Slot *sl) {
     cudaFreeHost(sl->h_out);
     cudaFreeHost(sl->h_status);
     if (sl->ev) cudaEventDestroy(sl->ev);
+    if (sl->ev_start) cudaEventDestroy(sl->ev_start);
+    if (sl->ev_end) cudaEventDestroy(sl->ev_end);
     delete sl;
 }
 
-// (re)size a slot for `cap` items and `msg_cap` message bytes
-// Slots are sized once for a full batch; the message area grows
-// geometrically, so re-creation (whose cudaFree would wait for the whole
-// device) is rare.
-static bool size_slot(cuspx_server *s, Group &g, Slot *sl, size_t cap, size_t msg_cap) {
+static size_t class_msg_bytes(const cuspx_server *s, const Group &g) {
+    return g.long_class ? kLongLaunchBytes : (size_t)s->cfg.max_batch * (kLongMsg + 16);
+}
+
+// Create a slot's batch and pinned staging once, at the full size of its
+// group (max_batch items, the class's message area).
+static bool size_slot(cuspx_server *s, Group &g, Slot *sl) {
     const SetParams &P = g.P;
-    if (sl->b && sl->cap >= cap && sl->msg_cap >= msg_cap) return true;
-    cap = std::max<size_t>(std::max(cap, sl->cap), (size_t)s->cfg.max_batch);
-    size_t want = std::max<size_t>(sl->msg_cap ? 2 * sl->msg_cap : (size_t)4 << 20, msg_cap);
-    msg_cap = want;
-    if (sl->b) {
-        cuspx_batch_destroy(sl->b);
-        sl->b = nullptr;
-    }
+    if (sl->b) return true;
+    const size_t cap = (size_t)s->cfg.max_batch;
+    const size_t msg_cap = class_msg_bytes(s, g);
     if (cuspx_batch_create(s->ctx, g.op, g.set, cap, msg_cap, 1, &sl->b) != CUSPX_OK) return false;
+    // short-message launches run ahead of long-message ones on the GPU
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    batch_set_stream_priority(sl->b, g.long_class ? lo : hi);
     const KeyTable &kt = s->keys[g.set];
     cuspx_batch_bind_keys(sl->b, g.op == CUSPX_OP_SIGN ? kt.d_sk : kt.d_pk, kt.cap);
-    auto host = [](void **p, size_t bytes) { cudaFreeHost(*p); return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };
+    auto host = [](void **p, size_t bytes) { return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };
     bool ok = host((void **)&sl->h_msg, msg_cap + 64) && host((void **)&sl->h_off, cap * 8) &&
               host((void **)&sl->h_len, cap * 8) && host((void **)&sl->h_siglen, cap * 8) &&
               host((void **)&sl->h_kidx, cap * 4) &&
               host((void **)&sl->h_aux, g.op == CUSPX_OP_VERIFY ? cap * P.sig_bytes : 16) &&
               host((void **)&sl->h_out, g.op == CUSPX_OP_SIGN ? cap * P.sig_bytes : 16) &&
               host((void **)&sl->h_status, cap * 4);
-    if (!sl->ev) cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming);
+    cudaEventCreate(&sl->ev_start);
+    cudaEventCreate(&sl->ev_end);
     sl->cap = cap;
     sl->msg_cap = msg_cap;
     return ok;
@@ -175,9 +187,9 @@ static bool size_slot(cuspx_server *s, Group &g, Slot *sl, size_t cap, size_t ms
 // pack requests into the slot's pinned staging and launch asynchronously
 static bool launch_slot(cuspx_server *s, Group &g, Slot *sl) {
     const SetParams &P = g.P;
-    size_t total = 0;
-    for (Req *r : sl->reqs) total += (r->mlen + 15) & ~(size_t)15;
-    if (!size_slot(s, g, sl, sl->reqs.size(), total)) return false;
+    if (!size_slot(s, g, sl)) return false;
+    cudaStream_t st = (cudaStream_t)cuspx_batch_stream(sl->b);
+    cudaEventRecord(sl->ev_start, st);
     size_t off = 0;
     for (size_t i = 0; i < sl->reqs.size(); i++) {
         Req *r = sl->reqs[i];
@@ -203,13 +215,19 @@ static bool launch_slot(cuspx_server *s, Group &g, Slot *sl) {
     if (cuspx_batch_download_async(sl->b, g.op == CUSPX_OP_SIGN ? sl->h_out : nullptr, nullptr, sl->h_status) !=
         CUSPX_OK)
         return false;
-    return cudaEventRecord(sl->ev, (cudaStream_t)cuspx_batch_stream(sl->b)) == cudaSuccess;
+    cudaEventRecord(sl->ev_end, st);
+    return cudaEventRecord(sl->ev, st) == cudaSuccess;
 }
 
 // mark a slot's requests done (called with the lock held)
 static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
     const SetParams &P = g.P;
     const auto now = Clock::now();
+    float lms = 0;
+    if (ok && sl->ev_start && cudaEventElapsedTime(&lms, sl->ev_start, sl->ev_end) == cudaSuccess) {
+        s->launch_ms_sum += lms;
+        s->launch_ms_max = std::max<double>(s->launch_ms_max, lms);
+    }
     for (size_t i = 0; i < sl->reqs.size(); i++) {
         Req *r = sl->reqs[i];
         r->status = ok ? sl->h_status[i] : -3;
@@ -288,11 +306,16 @@ static void scheduler(cuspx_server *s) {
                     free_sl = new Slot();
                     g.slots.push_back(free_sl);
                 }
-                // take as many as fit the batch size and the memory budget
-                size_t n = 0, bytes = 0;
+                // take as many as fit the batch size, the launch's message
+                // area and the memory budget
+                size_t n = 0, bytes = 0, mbytes = 0;
+                const size_t mcap = class_msg_bytes(s, g);
                 for (Req *r : g.pending) {
                     if (n == (size_t)s->cfg.max_batch) break;
-                    const size_t add = g.per_item + ((r->mlen + 15) & ~(size_t)15);
+                    const size_t m16 = (r->mlen + 15) & ~(size_t)15;
+                    if (mbytes + m16 > mcap) break;
+                    mbytes += m16;
+                    const size_t add = g.per_item + m16;
                     if (s->bytes_inflight + bytes + add > s->cfg.mem_budget && n > 0) break;
                     if (s->bytes_inflight + bytes + add > s->cfg.mem_budget && s->bytes_inflight > 0) break;
                     bytes += add;
@@ -445,6 +468,7 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     if (s->stop) rc = CUSPX_EBUSY;
     else if (key_id >= kt.n || (op == CUSPX_OP_SIGN && !kt.has_sk[key_id])) rc = CUSPX_EINVAL;
     else if (g.per_item + mlen > s->cfg.mem_budget) rc = CUSPX_ENOMEM;
+    else if (mlen + 16 > kLongLaunchBytes) rc = CUSPX_ETOOBIG;
     else if (s->pending_total >= s->cfg.max_queue) rc = CUSPX_EBUSY;
     if (rc != CUSPX_OK) {
         s->refused++;
@@ -505,6 +529,8 @@ int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st) {
         st->bytes_inflight = s->bytes_inflight;
         st->bytes_peak = s->bytes_peak;
         st->mean_batch = s->launches ? (double)s->batched / s->launches : 0.0;
+        st->launch_ms_mean = s->launches ? s->launch_ms_sum / s->launches : 0.0;
+        st->launch_ms_max = s->launch_ms_max;
         ls = s->lat_sign;
         lv = s->lat_verify;
     }
@@ -528,6 +554,7 @@ int cuspx_serve_reset_stats(cuspx_server *s) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->submitted = s->completed = s->refused = s->failed = s->launches = s->batched = 0;
     s->sign_done = s->verify_done = s->wrong = 0;
+    s->launch_ms_sum = s->launch_ms_max = 0;
     s->bytes_peak = s->bytes_inflight;
     s->lat_sign.clear();
     s->lat_verify.clear();
@@ -654,6 +681,8 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
     out->verify_p50_us = st.verify_p50_us;
     out->verify_p99_us = st.verify_p99_us;
     out->mean_batch = st.mean_batch;
+    out->launch_ms_mean = st.launch_ms_mean;
+    out->launch_ms_max = st.launch_ms_max;
     for (int b = 0; b < 3; b++) {
         out->sign_p50_bucket_us[b] = st.sign_p50_bucket_us[b];
         out->sign_p99_bucket_us[b] = st.sign_p99_bucket_us[b];

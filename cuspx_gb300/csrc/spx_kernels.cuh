@@ -80,6 +80,8 @@ struct SignArgs {
     uint8_t *roots;            // count x d x n
     uint8_t *chains;           // count x d x len x 16 x n  (signing leaf's chain values)
     int32_t *status;           // count
+    uint8_t *ends = nullptr;   // chain-parallel scratch: ends_cap x d x 2^hp x len x n, or null
+    uint32_t ends_cap = 0;
 };
 
 // tree/leaf indices of hypertree layer L (sign.cu:1987-1988)
@@ -276,6 +278,7 @@ struct LeafArgs {
     const SignWork *work;  // null for key generation (tree 0, no signing leaf)
     uint8_t *leaves;     // [item][layer-layer0][leaf] n bytes
     uint8_t *chains;     // [item][layer][chain][16] n bytes, or null
+    uint8_t *ends;       // chain-parallel mode: [item][layer-layer0][leaf][chain] n bytes
 };
 
 template <class HF>
@@ -332,6 +335,102 @@ __global__ void __launch_bounds__(256, HF::kLeafMinBlocks) k_leaves(SetParams P,
     uint32_t leaf[W];
     HF::t_final(leaf, ts);
     HF::store(A.leaves + (((uint64_t)item * A.nlayers + (L - A.layer0)) * nleaf + j) * N, leaf);
+}
+
+// ===========================================================================
+// XMSS leaves, chain-parallel mode (small batches): one thread per WOTS+
+// chain (wots_gen_pk's loop body, wots.cu:181-184) writes its chain end;
+// then one thread per leaf hashes the len ends with T_len.  35x (n=16) the
+// threads of k_leaves, so a few signatures still fill the GPU; the cost is
+// the chain-end round trip through memory and an idle T_len pass for most
+// lanes, which is why big batches use k_leaves.
+// ===========================================================================
+template <class HF>
+__global__ void k_leaf_chains(SetParams P, LeafArgs A) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nleaf = 1u << P.hp;
+    const uint64_t per_item = (uint64_t)A.nlayers * nleaf * LEN;
+    if (gid >= (uint64_t)A.count * per_item) return;
+    const uint32_t item = (uint32_t)(gid / per_item);
+    uint32_t rem = (uint32_t)(gid % per_item);
+    const int c = (int)(rem % LEN);
+    rem /= LEN;
+    const uint32_t j = rem & (nleaf - 1);
+    const int Lr = (int)(rem >> P.hp);
+    const int L = A.layer0 + Lr;
+    const uint8_t *sk = A.sk.row(item);
+    KeyRegs<N> key;
+    uint64_t tree_L = 0;
+    uint32_t idx_L = 0xffffffffu;
+    if (A.work) {
+        const SignWork wk = A.work[item];
+        key_from_work<HF>(key, sk, sk + 2 * N, wk);
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    } else {
+        HF::key_init(key, sk, sk + 2 * N);
+    }
+    const bool rec = A.chains && (j == idx_L);
+    uint8_t *chain = rec ? A.chains + ((((uint64_t)item * P.d + L) * LEN + c) * 16) * N : nullptr;
+    Adrs wa;
+    adrs_zero(wa);
+    adrs_layer(wa, L);
+    adrs_tree(wa, tree_L);
+    adrs_type(wa, ADDR_WOTS);
+    adrs_keypair(wa, j);
+    adrs_chain(wa, c);
+    adrs_hash(wa, 0);
+    uint32_t v[W];
+    HF::PRF(v, wa, key);
+    if (rec) HF::store(chain, v);
+    typename HF::FCtx fc;
+    HF::f_prepare(fc, wa, key);
+    for (int s = 0; s < 15; s++) {
+        HF::f_step(v, v, fc, s, key);
+        if (rec) HF::store(chain + (uint64_t)(s + 1) * N, v);
+    }
+    HF::store(A.ends + gid * N, v);
+}
+
+template <class HF>
+__global__ void k_leaf_tlen(SetParams P, LeafArgs A) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    extern __shared__ uint32_t smem[];
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nleaf = 1u << P.hp;
+    if (gid >= (uint64_t)A.count * A.nlayers * nleaf) return;
+    const uint32_t item = (uint32_t)(gid / ((uint64_t)A.nlayers * nleaf));
+    const uint32_t rem = (uint32_t)(gid % ((uint64_t)A.nlayers * nleaf));
+    const int L = A.layer0 + (int)(rem >> P.hp);
+    const uint32_t j = rem & (nleaf - 1);
+    const uint8_t *sk = A.sk.row(item);
+    KeyRegs<N> key;
+    uint64_t tree_L = 0;
+    uint32_t idx_L = 0;
+    if (A.work) {
+        const SignWork wk = A.work[item];
+        key_from_work<HF>(key, sk, sk + 2 * N, wk);
+        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    } else {
+        HF::key_init(key, sk, sk + 2 * N);
+    }
+    Adrs pa;
+    adrs_zero(pa);
+    adrs_layer(pa, L);
+    adrs_tree(pa, tree_L);
+    adrs_type(pa, ADDR_WOTSPK);
+    adrs_keypair(pa, j);
+    typename HF::TStream ts;
+    HF::t_init(ts, smem + threadIdx.x * HF::kSmemWords, key, pa);
+    const uint8_t *e = A.ends + gid * LEN * N;
+    for (int c = 0; c < LEN; c++) {
+        uint32_t v[W];
+        HF::load(v, e + (uint64_t)c * N);
+        HF::t_absorb(ts, v, key);
+    }
+    uint32_t leaf[W];
+    HF::t_final(leaf, ts);
+    HF::store(A.leaves + gid * N, leaf);
 }
 
 // ===========================================================================

@@ -20,6 +20,7 @@ struct Tuning {
     int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers
     int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
+    int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
 };
 
 struct KeygenArgs {
@@ -28,6 +29,8 @@ struct KeygenArgs {
     uint8_t *pk;       // count x 2n: written
     uint8_t *leaves;   // count x 2^hp x n scratch
     uint8_t *roots;    // count x n scratch
+    uint8_t *ends;     // chain-parallel scratch (count x 2^hp x len x n) or null
+    uint32_t ends_cap; // items the chain-parallel scratch holds
 };
 
 // Optional per-kernel timing: an event is recorded on the launch stream
@@ -86,6 +89,7 @@ struct Family {
         cudaError_t e;
         const int big = 200 * 1024;
         if ((e = cudaFuncSetAttribute(k_leaves<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_leaf_tlen<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_fors_sign<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_trees<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_verify_ht<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
@@ -107,6 +111,24 @@ struct Family {
         k_trees<HF><<<ceil_div(warps, wpb), 32 * wpb, per_warp * wpb, s>>>(P, T);
     }
 
+    // XMSS leaves: one thread per leaf (k_leaves), or for small batches one
+    // thread per chain then one per leaf (k_leaf_chains + k_leaf_tlen)
+    static void leaves(const SetParams &P, const LeafArgs &L, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
+                       bool chain_mode) {
+        const uint64_t nleaves = (uint64_t)L.count * L.nlayers * (1u << P.hp);
+        if (chain_mode) {
+            constexpr int LEN = 2 * N + 3;
+            k_leaf_chains<HF><<<ceil_div(nleaves * LEN, 128), 128, 0, s>>>(P, L);
+            CUSPX_MARK(pt, "k_leaf_chains", s);
+            k_leaf_tlen<HF><<<ceil_div(nleaves, 64), 64, (size_t)64 * HF::kSmemWords * 4, s>>>(P, L);
+            CUSPX_MARK(pt, "k_leaf_tlen", s);
+            return;
+        }
+        const int b = tu.leaf_block;
+        k_leaves<HF><<<ceil_div(nleaves, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, L);
+        CUSPX_MARK(pt, "k_leaves", s);
+    }
+
     static void sign(const SetParams &P, const SignArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
         if (A.count == 0) return;
         k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
@@ -122,11 +144,8 @@ struct Family {
             CUSPX_MARK(pt, "k_fors_sign", s);
         }
         {
-            LeafArgs L{A.count, 0, P.d, A.sk, A.work, A.leaves, A.chains};
-            const int b = tu.leaf_block;
-            const uint64_t threads = (uint64_t)A.count * P.d * (1u << P.hp);
-            k_leaves<HF><<<ceil_div(threads, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, L);
-            CUSPX_MARK(pt, "k_leaves", s);
+            LeafArgs L{A.count, 0, P.d, A.sk, A.work, A.leaves, A.chains, A.ends};
+            leaves(P, L, tu, s, pt, A.ends && A.count <= (uint32_t)tu.chain_mode_max && A.count <= A.ends_cap);
         }
         {
             TreeArgs T{A.count, 0, P.d, A.sk, A.work, A.leaves, A.roots, A.sig};
@@ -165,11 +184,8 @@ struct Family {
     static void keygen(const SetParams &P, const KeygenArgs &K, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
         if (K.count == 0) return;
         KeyRef kr{K.sk, nullptr, (uint32_t)(4 * N)};
-        LeafArgs L{K.count, P.d - 1, 1, kr, nullptr, K.leaves, nullptr};
-        const int b = tu.leaf_block;
-        const uint64_t threads = (uint64_t)K.count * (1u << P.hp);
-        k_leaves<HF><<<ceil_div(threads, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, L);
-        CUSPX_MARK(pt, "k_leaves", s);
+        LeafArgs L{K.count, P.d - 1, 1, kr, nullptr, K.leaves, nullptr, K.ends};
+        leaves(P, L, tu, s, pt, K.ends && K.count <= (uint32_t)tu.chain_mode_max * P.d && K.count <= K.ends_cap);
         TreeArgs T{K.count, P.d - 1, 1, kr, nullptr, K.leaves, K.roots, nullptr};
         trees(P, T, tu, s);
         CUSPX_MARK(pt, "k_trees", s);

@@ -18,7 +18,7 @@
 #include "spx_hash.cuh"
 
 #ifndef CUSPX_ROBUST_LEAF_MINBLOCKS
-#define CUSPX_ROBUST_LEAF_MINBLOCKS 2
+#define CUSPX_ROBUST_LEAF_MINBLOCKS 1
 #endif
 
 namespace cuspx {
@@ -73,8 +73,9 @@ struct Sha2 {
     static constexpr int W = N / 4;
     static constexpr bool kRobust = ROBUST;
     static constexpr int kShake = 0;
-    // k_leaves register budget: robust chains carry a second (mask) state and
-    // would otherwise leave only 2-3 blocks per SM
+    // k_leaves occupancy floor for robust chains (which carry a second, mask
+    // state); measured on GB300, capping registers to raise it spills and is
+    // slower, so the default leaves the compiler's choice
     static constexpr int kLeafMinBlocks = ROBUST ? CUSPX_ROBUST_LEAF_MINBLOCKS : 1;
 
     // memory <-> register order

@@ -70,9 +70,11 @@ typedef struct {
     int verify_mode;      /* 0 layered verify kernels, 1 one thread per item over all layers */
     int fors_lanes_log2;  /* lanes per FORS tree = 2^g, g in 0..5 (0: lane per tree, 5: warp per tree) */
     int tree_mode;        /* 0 warp per XMSS subtree, 1 lane per subtree (heights <= 4 only) */
+    int chain_mode_max;   /* batches of at most this many signatures (up to 256) compute XMSS
+                             leaves one lane per WOTS+ chain instead of one lane per leaf */
 } cuspx_tuning;
-/* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2
- * and tree_mode, which keep it when < 0 */
+/* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2,
+ * tree_mode and chain_mode_max, which keep it when < 0 */
 int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
 int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
 

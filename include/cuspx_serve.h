@@ -15,7 +15,9 @@
  *     launches stay within `mem_budget`; submissions beyond `max_queue`
  *     pending requests are refused with CUSPX_EBUSY;
  *   - requests with messages over 16 KiB are batched apart from shorter ones
- *     (their serial message hashing would hold a shared batch back);
+ *     (their serial message hashing would hold a shared batch back); a
+ *     launch carries at most 64 MiB of long messages, and a single message
+ *     over 64 MiB is refused with CUSPX_ETOOBIG;
  *   - per-request latency (submit to result on the host) feeds p50/p99,
  *     overall and per message-length bucket.
  * Results of a request do not depend on what it was batched with.
@@ -52,6 +54,7 @@ typedef struct {
     /* latency by message length: [0] <= 1 KiB, [1] <= 64 KiB, [2] > 64 KiB */
     double sign_p50_bucket_us[3], sign_p99_bucket_us[3], verify_p50_bucket_us[3], verify_p99_bucket_us[3];
     uint64_t bucket_count[2][3];   /* [sign, verify][bucket] */
+    double launch_ms_mean, launch_ms_max;   /* device time of a launch: upload + kernels + download */
 } cuspx_serve_counters;
 
 /* submit flags */
@@ -98,6 +101,7 @@ typedef struct {
     double sign_p50_us, sign_p99_us, verify_p50_us, verify_p99_us;
     double mean_batch;
     double sign_p50_bucket_us[3], sign_p99_bucket_us[3], verify_p50_bucket_us[3], verify_p99_bucket_us[3];
+    double launch_ms_mean, launch_ms_max;
 } cuspx_loadgen_result;
 
 int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *cfg, cuspx_loadgen_result *out);

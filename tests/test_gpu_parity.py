@@ -173,14 +173,16 @@ def test_sign_mappings_agree(engine, setname):
     saved = engine.get_tuning(sid)
     ref = None
     try:
-        for g, tm, lb, fb in ((5, 0, 128, 128), (0, 1, 64, 64), (2, 1, 256, 96), (3, 0, 96, 256)):
-            engine.set_tuning(sid, fors_lanes_log2=g, tree_mode=tm, leaf_block=lb, fors_block=fb)
+        for g, tm, lb, fb, cm in ((5, 0, 128, 128, 0), (0, 1, 64, 64, 64), (2, 1, 256, 96, 0),
+                                  (3, 0, 96, 256, 256)):
+            engine.set_tuning(sid, fors_lanes_log2=g, tree_mode=tm, leaf_block=lb, fors_block=fb,
+                              chain_mode_max=cm)
             sigs, st = engine.sign_batch(sid, [sk] * len(msgs), msgs)
             assert list(st) == [0] * len(msgs)
-            assert list(sigs[:2]) == want, (g, tm, lb, fb)
+            assert list(sigs[:2]) == want, (g, tm, lb, fb, cm)
             if ref is None:
                 ref = sigs
-            assert sigs == ref, (g, tm, lb, fb)
+            assert sigs == ref, (g, tm, lb, fb, cm)
     finally:
         engine.set_tuning(sid, **saved)
 

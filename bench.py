@@ -41,6 +41,17 @@ METRIC = "sign/s & verify/s, SHA2-128f, 1 GB300: batched+served vs plain; p50/p9
 # SHA-256 compressions per XMSS leaf for 128f (35 chains x (PRF + 15 F) + 10 T_len blocks)
 LEAF_CMP = {16: 35 * 16 + 10, 24: 51 * 16 + 20, 32: 67 * 16 + 36}
 OPS_PER_CMP = 1384   # INT ops of one SHA-256 compression (64 rounds x 14 + 48 x 10 + 8)
+# SHA-256 compressions per 128f operation, message hashing excluded (<1% at the
+# message lengths used here): sign = FORS + d x (2^hp leaves + tree) + T_k,
+# verify = FORS roots + T_k + d x (chains + T_len + auth path)
+SIGN_CMP_128F = 113265
+VERIFY_CMP_128F = 6400
+
+
+def int_frac(signs, verifies, peak_ops):
+    """Fraction of the measured integer-ALU peak that `signs`/s and
+    `verifies`/s of SHA-256-128f-simple amount to."""
+    return (signs * SIGN_CMP_128F + verifies * VERIFY_CMP_128F) * OPS_PER_CMP / peak_ops
 
 
 def dist_env():
@@ -318,7 +329,7 @@ def main():
 
     served = None
     if rank == 0 and not args.no_served:
-        served = served_runs(c, eng)
+        served = served_runs(c, eng, peak_ops)
     extra = {}
     if rank == 0 and not args.no_extra:
         extra["uneven_mixed"] = uneven_mixed(c, eng)
@@ -340,7 +351,9 @@ def main():
                        "l2": "256 MiB buffer written between timed steps (L2 is 129 MB)",
                        "subset_check": "%d seeded signatures byte-identical to the CPU oracle" % SUBSET,
                        "mapping": tuned},
-            "verify": {"value": verify_value, "unit": "verify/s", "ms_per_batch": verify_total / args.steps},
+            "verify": {"value": verify_value, "unit": "verify/s", "ms_per_batch": verify_total / args.steps,
+                       "roofline_frac": int_frac(0, verify_value, peak_ops)},
+            "step_roofline_frac": int_frac(value, 0, peak_ops),
             "e2e": {"value": e2e_value, "unit": "sign/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_total / args.steps},
             "gpu_launches": (5 + 3) * args.steps,
@@ -378,7 +391,7 @@ def main():
     return 0
 
 
-def served_runs(c, eng, seconds=2.0):
+def served_runs(c, eng, peak_ops, seconds=2.0):
     """Open-loop Poisson streams through the serving loop (cuspx_serve_*).
 
     served_128f: SHA-256-128f-simple only, 30% sign / 70% verify, 64 resident
@@ -397,14 +410,17 @@ def served_runs(c, eng, seconds=2.0):
     srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000)
     srv.add_keys(sid, sks)
     pts = []
-    for rate in (5e3, 20e3, 50e3, 100e3, 200e3):
+    # 300k and 400k req/s offered are past what the GPU can serve at this mix
+    # (~430k req/s of pure compute): they show the served roofline fraction
+    for rate in (5e3, 20e3, 50e3, 100e3, 200e3, 300e3, 400e3):
         r = srv.loadgen(rate, seconds, [sid], 64, verify_frac=0.7, min_len=16, max_len=1024, corrupt_frac=0.1,
                         seed=int(rate), pool=512)
         pts.append({"rate": rate, "sign_per_s": r["sign_throughput"], "verify_per_s": r["verify_throughput"],
                     "sign_p50_ms": r["sign_p50_us"] / 1e3, "sign_p99_ms": r["sign_p99_us"] / 1e3,
                     "verify_p50_ms": r["verify_p50_us"] / 1e3, "verify_p99_ms": r["verify_p99_us"] / 1e3,
                     "completed": r["completed"], "refused": r["refused"], "wrong_verdicts": r["wrong_verdicts"],
-                    "mean_batch": r["mean_batch"]})
+                    "mean_batch": r["mean_batch"],
+                    "roofline_frac": int_frac(r["sign_throughput"], r["verify_throughput"], peak_ops)})
     srv.close()
     out["served_128f"] = pts
     names = ["sha256-128f-simple", "sha256-192f-simple", "shake256-256f-simple"]

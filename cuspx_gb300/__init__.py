@@ -39,7 +39,7 @@ class Tuning(ctypes.Structure):
     """cuspx_tuning: the launch mapping of one parameter set."""
     _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
                                             "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode",
-                                            "chain_mode_max")]
+                                            "chain_mode_max", "verify_slots")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -189,7 +189,7 @@ class Engine:
 
     def set_tuning(self, sid, **kw):
         """Change fields of a set's launch mapping (others keep their value)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")

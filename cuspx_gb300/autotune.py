@@ -8,7 +8,8 @@ real batches on the device:
   sign:   chain_mode_max (lane per chain vs lane per leaf for this batch
           size), fors_lanes_log2 (lanes per FORS tree), tree_mode,
           leaf_block, fors_block, tree_warps
-  verify: chains_per_warp, verify_block, verify_mode
+  verify: verify_mode (layered kernels or one persistent launch), and for
+          each the chains per warp / items per warp and block size
 
 Search is coordinate descent: each knob is swept with the others held, the
 best value kept, for two passes.  Every candidate is timed with CUDA events
@@ -32,9 +33,10 @@ SIGN_SPACE = {
     "tree_warps": [1, 2, 4],
 }
 VERIFY_SPACE = {
+    "verify_mode": [0, 1, 2],
+    "verify_slots": [2, 3, 4, 6, 8],
     "chains_per_warp": [32, 64, 128, 256, 512],
     "verify_block": [32, 64, 128],
-    "verify_mode": [0, 1],
 }
 
 

@@ -125,6 +125,7 @@ struct cuspx_batch {
     SignWork *work = nullptr;
     uint8_t *fors_roots = nullptr, *leaves = nullptr, *roots = nullptr, *chains = nullptr;
     uint8_t *wpk = nullptr, *cur_root = nullptr;
+    uint32_t *ctr = nullptr;   // persistent verify item counter
     uint8_t *ends = nullptr;   // chain-parallel leaf scratch
     uint32_t ends_cap = 0;
     size_t count = 0;
@@ -229,6 +230,7 @@ int cuspx_create(int device, cuspx_ctx **out) {
         t.tree_mode = sd.h / sd.d <= 4 ? 1 : 0;
         t.leaf_block = (sd.hash == 0 && !sd.robust) ? 256 : 128;
         t.chains_per_warp = sd.hash == 1 ? 256 : 128;
+        t.verify_mode = (sd.hash == 0 && !sd.robust) ? 2 : 0;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;
@@ -280,7 +282,7 @@ int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
         t.chains_per_warp = in->chains_per_warp;
     }
     if (in->verify_mode >= 0) {
-        if (in->verify_mode > 1) return fail(ctx, CUSPX_EINVAL, "verify_mode must be 0 or 1");
+        if (in->verify_mode > 2) return fail(ctx, CUSPX_EINVAL, "verify_mode must be 0, 1 or 2");
         t.verify_mode = in->verify_mode;
     }
     if (in->fors_lanes_log2 >= 0) {
@@ -292,6 +294,10 @@ int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
         t.tree_mode = in->tree_mode;
     }
     if (in->chain_mode_max >= 0) t.chain_mode_max = in->chain_mode_max;
+    if (in->verify_slots > 0) {
+        if (in->verify_slots > 8) return fail(ctx, CUSPX_EINVAL, "verify_slots must be in 1..8");
+        t.verify_slots = in->verify_slots;
+    }
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->tune[set] = t;   // batches re-capture their graph when the mapping changed
     return CUSPX_OK;
@@ -309,6 +315,7 @@ int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
     out->fors_lanes_log2 = t.fors_lanes_log2;
     out->tree_mode = t.tree_mode;
     out->chain_mode_max = t.chain_mode_max;
+    out->verify_slots = t.verify_slots;
     return CUSPX_OK;
 }
 
@@ -394,6 +401,7 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
             A((void **)&b->siglen, cap * sizeof(uint64_t));
             A((void **)&b->wpk, cap * P.len * n);
             A((void **)&b->cur_root, cap * n);
+            A((void **)&b->ctr, 16);
         }
     }
     if (rc != CUSPX_OK) {
@@ -511,6 +519,7 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.verdict = b->status;
         A.wpk = b->wpk;
         A.cur_root = b->cur_root;
+        A.ctr = b->ctr;
         ops.verify(P, A, tu, b->s, pt);
     } else {
         KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots, b->ends, b->ends_cap};

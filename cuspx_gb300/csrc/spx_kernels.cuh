@@ -666,6 +666,7 @@ struct VerifyArgs {
     int32_t *verdict;           // 0 accept, -1 reject (crypto_sign_verify)
     uint8_t *wpk;               // count x len x n: WOTS public key of the current layer
     uint8_t *cur_root;          // count x n: root of the layer below (FORS key for layer 0)
+    uint32_t *ctr = nullptr;    // persistent verify: next item to take (zeroed per launch)
 };
 
 template <class HF>

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "spx_kernels.cuh"
+#include "spx_verify.cuh"
 
 namespace cuspx {
 
@@ -17,10 +18,12 @@ struct Tuning {
     int verify_block = 64;   // threads per block for k_verify_root (and k_verify_ht)
     int tree_warps = 4;      // warps per block for k_trees (upper bound)
     int chains_per_warp = 64;  // (item, chain) tasks per warp in k_verify_chains
-    int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers
+    int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers,
+                             // 2 persistent hypertree kernel (SHA-256 simple sets)
     int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
+    int verify_slots = 4;    // items per warp in the persistent verify kernel
 };
 
 struct KeygenArgs {
@@ -94,7 +97,36 @@ struct Family {
         if ((e = cudaFuncSetAttribute(k_trees<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_verify_ht<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_verify_root<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if constexpr (kPersistVerify)
+            if ((e = cudaFuncSetAttribute(k_verify_hyper<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big)))
+                return e;
         return cudaSuccess;
+    }
+
+    // the persistent verify kernel covers the SHA-256 simple sets
+    static constexpr bool kPersistVerify = !HF::kShake && !HF::kRobust;
+
+    // one launch over the batch's whole hypertree: as many blocks as are
+    // resident at once (or fewer for small batches); warps take items from
+    // the counter as their slots free up
+    static void verify_persistent(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s,
+                                  PhaseTimer *pt) {
+        if constexpr (kPersistVerify) {
+            int wpb = tu.verify_block / 32;
+            wpb = wpb < 1 ? 1 : (wpb > 4 ? 4 : wpb);
+            const int G = tu.verify_slots < 1 ? 1 : (tu.verify_slots > 8 ? 8 : tu.verify_slots);
+            const size_t smem = (size_t)wpb * G * PersistVerify<HF>::slot_words(P.hp) * 4;
+            int dev = 0, sms = 0, occ = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_verify_hyper<HF>, 32 * wpb, smem);
+            if (occ < 1) occ = 1;
+            const uint64_t want = ceil_div(A.count, (uint64_t)G * wpb);
+            const uint64_t cap = (uint64_t)occ * (sms > 0 ? sms : 1);
+            cudaMemsetAsync(A.ctr, 0, sizeof(uint32_t), s);
+            k_verify_hyper<HF><<<(unsigned)(want < cap ? want : cap), 32 * wpb, smem, s>>>(P, A, A.ctr, G);
+            CUSPX_MARK(pt, "k_verify_hyper", s);
+        }
     }
 
     static void trees(const SetParams &P, const TreeArgs &T, const Tuning &tu, cudaStream_t s) {
@@ -163,6 +195,10 @@ struct Family {
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_verify_fors", s);
         const int b = tu.verify_block;
+        if (tu.verify_mode == 2 && kPersistVerify && A.ctr) {
+            verify_persistent(P, A, tu, s, pt);
+            return;
+        }
         if (tu.verify_mode == 1) {
             k_verify_ht<HF><<<ceil_div(A.count, b), b, (size_t)b * HF::kSmemWords * 4, s>>>(P, A);
             CUSPX_MARK(pt, "k_verify_ht", s);

@@ -132,7 +132,8 @@ def test_sign_status_flags_bad_key(engine):
     assert list(st) == [0, -2]
 
 
-@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-simple", "sha256-192f-robust"])
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-simple", "sha256-192f-robust",
+                                     "sha256-192f-simple", "sha256-256f-simple", "sha256-128s-simple"])
 def test_verify_mappings_agree(engine, setname):
     """Every verify launch mapping the autotuner may pick returns the same verdicts."""
     o = _oracle(setname)
@@ -152,10 +153,51 @@ def test_verify_mappings_agree(engine, setname):
     assert want.count(-1) == 3
     saved = engine.get_tuning(sid)
     try:
-        for mode, cpw in ((0, 32), (0, 64), (0, 1024), (1, 0)):
-            engine.set_tuning(sid, verify_mode=mode, **({"chains_per_warp": cpw} if cpw else {}))
+        for m in ({"verify_mode": 0, "chains_per_warp": 32}, {"verify_mode": 0, "chains_per_warp": 64},
+                  {"verify_mode": 0, "chains_per_warp": 1024}, {"verify_mode": 1},
+                  {"verify_mode": 2, "verify_slots": 1, "verify_block": 32},
+                  {"verify_mode": 2, "verify_slots": 3, "verify_block": 64},
+                  {"verify_mode": 2, "verify_slots": 8, "verify_block": 128}):
+            engine.set_tuning(sid, **m)
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
-            assert list(got) == want, (mode, cpw)
+            assert list(got) == want, m
+    finally:
+        engine.set_tuning(sid, **saved)
+
+
+def test_persistent_verify_refills_slots(engine):
+    """A batch larger than all resident warp slots together: warps take new
+    items from the counter as items finish; every verdict is still the CPU's
+    (intact, corrupted and wrong-length signatures interleaved)."""
+    setname = "sha256-128f-simple"
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(7)
+    seed = bytes(rng.randrange(256) for _ in range(3 * o.p.n))
+    pk, sk = o.seed_keypair(seed)
+    msgs = [bytes(rng.randrange(256) for _ in range(40 + 7 * i)) for i in range(3)]
+    sigs = [o.sign(m, sk) for m in msgs]
+    bad = []
+    for s in sigs:
+        b = bytearray(s)
+        b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
+        bad.append(bytes(b))
+    cases = []   # (sig, msg, siglen, expected)
+    for i in range(3):
+        cases.append((sigs[i], msgs[i], len(sigs[i]), o.verify(sigs[i], msgs[i], pk)))
+        cases.append((bad[i], msgs[i], len(bad[i]), o.verify(bad[i], msgs[i], pk)))
+        cases.append((sigs[i], msgs[i], len(sigs[i]) - 1, -1))
+    assert [c[3] for c in cases].count(0) == 3
+    count = 6000   # > 152 SMs x 32 resident one-warp blocks x 1 slot
+    pick = [rng.randrange(len(cases)) for _ in range(count)]
+    saved = engine.get_tuning(sid)
+    try:
+        for m in ({"verify_mode": 2, "verify_slots": 1, "verify_block": 32},
+                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 128}):
+            engine.set_tuning(sid, **m)
+            got = engine.verify_batch(sid, [pk] * count, [cases[j][1] for j in pick], [cases[j][0] for j in pick],
+                                      siglens=[cases[j][2] for j in pick])
+            assert list(got) == [cases[j][3] for j in pick], m
     finally:
         engine.set_tuning(sid, **saved)
 

@@ -23,7 +23,7 @@ struct Tuning {
     int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
-    int verify_slots = 4;    // items per warp in the persistent verify kernel
+    int verify_slots = 4;    // most items per warp in the persistent verify kernel
 };
 
 struct KeygenArgs {
@@ -114,11 +114,19 @@ struct Family {
         if constexpr (kPersistVerify) {
             int wpb = tu.verify_block / 32;
             wpb = wpb < 1 ? 1 : (wpb > 4 ? 4 : wpb);
-            const int G = tu.verify_slots < 1 ? 1 : (tu.verify_slots > 8 ? 8 : tu.verify_slots);
-            const size_t smem = (size_t)wpb * G * PersistVerify<HF>::slot_words(P.hp) * 4;
             int dev = 0, sms = 0, occ = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (sms < 1) sms = 1;
+            // Items per warp: one item's serial critical path (~d x 20
+            // compressions) sets the time of a small batch, and a warp
+            // holding several items runs their paths at a fraction of its
+            // lanes each, so a batch first spreads to about 4 warps per SM
+            // and only then packs up to verify_slots items per warp.
+            const int gmax = tu.verify_slots < 1 ? 1 : (tu.verify_slots > 8 ? 8 : tu.verify_slots);
+            int G = (int)ceil_div(A.count, 4ull * sms);
+            G = G < 1 ? 1 : (G > gmax ? gmax : G);
+            const size_t smem = (size_t)wpb * G * PersistVerify<HF>::slot_words(P.hp) * 4;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_verify_hyper<HF>, 32 * wpb, smem);
             if (occ < 1) occ = 1;
             const uint64_t want = ceil_div(A.count, (uint64_t)G * wpb);

@@ -74,7 +74,8 @@ typedef struct {
     int tree_mode;        /* 0 warp per XMSS subtree, 1 lane per subtree (heights <= 4 only) */
     int chain_mode_max;   /* batches of at most this many signatures (up to 256) compute XMSS
                              leaves one lane per WOTS+ chain instead of one lane per leaf */
-    int verify_slots;     /* items each warp holds at once in verify_mode 2 (1..8) */
+    int verify_slots;     /* most items a warp holds at once in verify_mode 2 (1..8); batches
+                             below about 4 warps per SM use fewer */
 } cuspx_tuning;
 /* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2,
  * tree_mode and chain_mode_max, which keep it when < 0 */

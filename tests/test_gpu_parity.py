@@ -161,6 +161,13 @@ def test_verify_mappings_agree(engine, setname):
             engine.set_tuning(sid, **m)
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
             assert list(got) == want, m
+        # a batch large enough that the persistent kernel packs several
+        # items into each warp (1300 items on 152 SMs: 3 per warp)
+        rep = 1300
+        engine.set_tuning(sid, verify_mode=2, verify_slots=8, verify_block=64)
+        got = engine.verify_batch(sid, [pks[kidx[i % 12]] for i in range(rep)], [msgs[i % 12] for i in range(rep)],
+                                  [sigs[i % 12] for i in range(rep)])
+        assert list(got) == [want[i % 12] for i in range(rep)]
     finally:
         engine.set_tuning(sid, **saved)
 

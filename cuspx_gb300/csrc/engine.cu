@@ -230,7 +230,7 @@ int cuspx_create(int device, cuspx_ctx **out) {
         t.tree_mode = sd.h / sd.d <= 4 ? 1 : 0;
         t.leaf_block = (sd.hash == 0 && !sd.robust) ? 256 : 128;
         t.chains_per_warp = sd.hash == 1 ? 256 : 128;
-        t.verify_mode = (sd.hash == 0 && !sd.robust) ? 2 : 0;
+        t.verify_mode = sd.robust ? 0 : 2;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;

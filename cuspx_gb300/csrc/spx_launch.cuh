@@ -19,7 +19,7 @@ struct Tuning {
     int tree_warps = 4;      // warps per block for k_trees (upper bound)
     int chains_per_warp = 64;  // (item, chain) tasks per warp in k_verify_chains
     int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers,
-                             // 2 persistent hypertree kernel (SHA-256 simple sets)
+                             // 2 persistent hypertree kernel (simple sets)
     int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
@@ -103,8 +103,8 @@ struct Family {
         return cudaSuccess;
     }
 
-    // the persistent verify kernel covers the SHA-256 simple sets
-    static constexpr bool kPersistVerify = !HF::kShake && !HF::kRobust;
+    // the persistent verify kernel covers the simple sets of both hashes
+    static constexpr bool kPersistVerify = !HF::kRobust;
 
     // one launch over the batch's whole hypertree: as many blocks as are
     // resident at once (or fewer for small batches); warps take items from
@@ -126,7 +126,7 @@ struct Family {
             const int gmax = tu.verify_slots < 1 ? 1 : (tu.verify_slots > 8 ? 8 : tu.verify_slots);
             int G = (int)ceil_div(A.count, 4ull * sms);
             G = G < 1 ? 1 : (G > gmax ? gmax : G);
-            const size_t smem = (size_t)wpb * G * PersistVerify<HF>::slot_words(P.hp) * 4;
+            const size_t smem = (size_t)wpb * G * VerifyPolicy<HF>::slot_words(P.hp) * 4;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_verify_hyper<HF>, 32 * wpb, smem);
             if (occ < 1) occ = 1;
             const uint64_t want = ceil_div(A.count, (uint64_t)G * wpb);

@@ -1,10 +1,10 @@
-// spx_verify.cuh -- persistent hypertree verify for the SHA-256 simple sets.
+// spx_verify.cuh -- persistent hypertree verify for the simple sets.
 //
 // crypto_sign_verify (sign.cu:3048-3121) is serial over the d layers of an
 // item: layer L's WOTS+ chains (wots_pk_from_sig, wots.cu:777-804) need the
 // root of layer L-1, T_len (sign.cu:3103) needs every chain end of layer L,
 // and compute_root (utils.cu:94-135) needs T_len.  Per item that is ~10-way
-// parallel work on average (35 chains, then one serial T_len + auth path),
+// parallel work on average (len chains, then one serial T_len + auth path),
 // so flat per-layer kernels leave the GPU idle during every T phase.
 //
 // Here one launch runs the whole hypertree for the batch.  Each warp owns G
@@ -12,48 +12,62 @@
 // any of its items offers:
 //
 //   chain   one F per iteration, from the signature value to step 15
-//   T       one 64-byte block of T_k (FORS key) or T_len per iteration
-//   root    one H compression of compute_root per iteration
+//   T       one block of T_k (FORS key) or T_len per iteration
+//   root    one H of compute_root per iteration (SHA-256 n >= 24: two blocks)
 //
-// T_len streams behind the chains: block j of ADRS_c || ends only needs the
-// chains whose end values it covers, so the T lane starts as soon as chains
-// 0..2 (n = 16) are done and takes each later block once its chains are; on
+// Every task is "one unit of the hash per iteration": a SHA-256 compression
+// from a state over a 16-word block, or a Keccak-f[1600] permutation of a
+// state with a 17-lane block absorbed.  Lanes differ only in how they build
+// the unit's input and use its output, so the hash itself -- the expensive
+// part -- runs converged across the warp whatever mix of tasks the lanes
+// hold.  Items are taken from a global counter as slots free up, so a batch
+// of any size keeps all warps busy.
+//
+// T streams behind the chains: block j of the T input only needs the chains
+// whose end values it covers, so the T lane starts as soon as the first
+// block's chains are done and takes each later block once its chains are; on
 // an iteration where its next block is not ready it idles.  This shortens an
-// item's per-layer critical path from ~15 + 10 + 3 to ~15 + 2 + 3
-// compressions, which is what lets few items per warp keep 32 lanes busy.
+// item's per-layer critical path from ~15 + |T| + h' to ~15 + 2 + h' units.
 //
-// Every task is "one SHA-256 compression from a state over a 16-word block";
-// lanes differ only in how they build (state, block) and use the output, so
-// the compression itself -- the expensive part -- runs converged across the
-// warp whatever mix of tasks the lanes hold.  Items are taken from a global
-// counter as slots free up, so a batch of any size keeps all warps busy.
-//
-// Slot data lives in shared memory: the T input stream (ADRS_c || values ||
+// Slot data lives in shared memory: the T input stream (prefix || values ||
 // padding, memory byte order) into which the layer's WOTS signature is
 // copied and where each chain's end value overwrites its start value in
-// place, the layer's auth path, the chain lengths, the key midstate and the
-// item's position.  Nothing waits on another warp; the loop ends when the
-// counter is exhausted and every slot is empty.
+// place, a bit per finished chain, the layer's auth path, the chain lengths,
+// the key material and the item's position (SHAKE also keeps the T sponge
+// state there).  Slots are private to their warp, so nothing waits on
+// another warp; the loop ends when the counter is exhausted and every slot
+// is empty.
+//
+// Items per warp: a small batch is bound by one item's serial path, so the
+// host launches one item per warp until there are about 4 warps per SM and
+// only then packs up to verify_slots items into a warp.
 #pragma once
+#include <type_traits>
+
 #include "spx_kernels.cuh"
 
 namespace cuspx {
 
-template <class HF>
-struct PersistVerify {
-    static constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
-    // T stream blocks after the key midstate: ADRS_c (22 B) || m values || pad
-    static constexpr int stream_blocks(int m) { return (22 + m * N + 9 + 63) / 64; }
-    static constexpr int kStreamWords = stream_blocks(LEN) * 16;
-    // H(left, right) = SHA256(midstate; ADRS_c || left || right): blocks
-    static constexpr int kHBlocks = (22 + 2 * N + 9 + 63) / 64;
-
+// Slot layout and bookkeeping shared by both hash families.  PRE is the
+// T stream's prefix in bytes (what is hashed before the first value) and
+// BLK its block size in bytes.
+template <int N_, int PRE, int BLK>
+struct VerifySlot {
+    static constexpr int N = N_, W = N / 4, LEN = 2 * N + 3;
     // slot header word indices
     enum : int {
-        S_ITEM = 0, S_LAYER, S_NEXT, S_DONE, S_TCLAIM, S_STATE, S_TREE_LO, S_TREE_HI, S_IDX_LEAF, S_IDXL,
-        S_AW0, S_AW1, S_AW2, S_M, S_NB,
-        S_ROOT = 16,     // W words
-        S_MID = 24,      // 8 words
+        S_ITEM = 0,      // batch index of the item
+        S_LAYER,         // -1: T_k over the FORS roots; 0..d-1: WOTS layer
+        S_NEXT,          // next chain to hand out
+        S_TCLAIM,        // the T stream has a lane
+        S_STATE,         // EMPTY / ACTIVE / ADVANCE / DEAD
+        S_TREE_LO, S_TREE_HI, S_IDX_LEAF,   // hypertree position from H_msg
+        S_IDXL,          // leaf index within the current layer's tree
+        S_AW0, S_AW1, S_AW2,                // ADRS words 0..2 of the current layer (type WOTS)
+        S_M,             // values in the current T stream (k or len)
+        S_NB,            // its blocks
+        S_ROOT = 16,     // W words: the message of the current layer
+        S_KEY = 24,      // 8 words: SHA-256 midstate of PUB_SEED, or PUB_SEED itself (SHAKE)
         S_LENS = 32,     // LEN bytes (17 words)
         S_MASK = 49,     // 3 words: bit c set when chain c's end value is in the stream
         S_HDR = 52,      // stream starts here (16-byte aligned)
@@ -61,11 +75,10 @@ struct PersistVerify {
     enum : uint32_t { EMPTY = 0, ACTIVE = 1, ADVANCE = 2, DEAD = 3 };
     enum : int { K_NONE = 0, K_CHAIN = 1, K_T = 2, K_ROOT = 3 };
 
-    static __host__ __device__ int slot_words(int hp) { return S_HDR + kStreamWords + hp * W; }
-
     // last value index that block j of a T stream over m values reads
     SPX_DEV static int block_last_value(int j, int m) {
-        const int last = (64 * j + 63 - 22) / N;
+        const int hi = BLK * (j + 1) - 1 - PRE;
+        const int last = hi < 0 ? -1 : hi / N;
         return last < m - 1 ? last : m - 1;
     }
     // number of leading finished chains (first clear bit of the 96-bit mask)
@@ -81,25 +94,48 @@ struct PersistVerify {
     static constexpr uint32_t mask_init(int q, int m) {
         return m <= 32 * q ? ~0u : (m >= 32 * (q + 1) ? 0u : ~0u << (m - 32 * q));
     }
+};
 
-    // -- byte-stream helpers (stream bytes in memory order, 32-bit words LE) --
+// ---------------------------------------------------------------------------
+// SHA-256: stream = ADRS_c (22 B) || values || SHA-256 padding, after the
+// PUB_SEED midstate; unit = one compression.  Values sit at offset 22 + c n
+// (2 mod 4), so they are read and written with byte permutes.
+// ---------------------------------------------------------------------------
+template <class HF>
+struct VerifySha2 : VerifySlot<4 * HF::W, 22, 64> {
+    using B = VerifySlot<4 * HF::W, 22, 64>;
+    static constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    static constexpr int stream_blocks(int m) { return (22 + m * N + 9 + 63) / 64; }
+    static constexpr int kStreamWords = stream_blocks(LEN) * 16;
+    static constexpr int kHBlocks = (22 + 2 * N + 9 + 63) / 64;   // H = SHA256(mid; ADRS_c || l || r)
+    static __host__ __device__ int slot_words(int hp) { return B::S_HDR + kStreamWords + hp * W; }
+
+    struct Unit {
+        uint32_t st[8], blk[16], out[8];
+    };
+    struct LaneRegs {
+        uint32_t kmid[8];   // the task's key midstate
+        uint32_t tst[8];    // T running state / first-block state of a two-block H
+    };
+
     SPX_DEV static void put16(uint32_t *base, int byte_off, uint32_t v) {
         reinterpret_cast<uint16_t *>(base)[byte_off >> 1] = (uint16_t)v;
     }
-    // value v (big-endian words) at a stream offset = 2 (mod 4)
-    SPX_DEV static void write_value(uint32_t *stream, int off, const uint32_t v[W]) {
+    // value c (big-endian words) at stream byte 22 + c n
+    SPX_DEV static void write_value(uint32_t *stream, int c, const uint32_t v[W]) {
+        const int off = 22 + c * N;
         put16(stream, off, __byte_perm(v[0], 0, 0x0023));
 #pragma unroll
         for (int i = 0; i + 1 < W; i++) stream[(off + 2) / 4 + i] = __byte_perm(v[i], v[i + 1], 0x6701);
         put16(stream, off + N - 2, __byte_perm(v[W - 1], 0, 0x0001));
     }
-    SPX_DEV static void read_value(const uint32_t *stream, int off, uint32_t v[W]) {
-        const int w0 = (off - 2) / 4;
+    SPX_DEV static void read_value(const uint32_t *stream, int c, uint32_t v[W]) {
+        const int w0 = (20 + c * N) / 4;
 #pragma unroll
         for (int i = 0; i < W; i++) v[i] = __byte_perm(stream[w0 + i], stream[w0 + i + 1], 0x2345);
     }
-    // copy `bytes` (multiple of 8) from 8-byte aligned global memory to the
-    // stream at offset 22, warp-cooperatively
+    // `bytes` (multiple of 8) from 8-byte aligned global memory to stream
+    // byte 22 onwards, warp-cooperatively
     SPX_DEV static void copy_values(uint32_t *stream, const uint8_t *src, int bytes, uint32_t lane) {
         for (int q = lane; q < bytes / 8; q += 32) {
             const uint2 x = reinterpret_cast<const uint2 *>(src)[q];
@@ -109,28 +145,83 @@ struct PersistVerify {
             put16(stream, o + 6, x.y >> 16);
         }
     }
-    // ADRS_c prefix (bytes 0..21) and padding after m values, for a T stream
-    // over m values: length counts the 64-byte midstate block
-    SPX_DEV static void stream_frame(uint32_t *stream, const Adrs &a, int m, uint32_t lane) {
-        const int end = 22 + m * N;                 // = 2 (mod 4)
-        const int nb = (end + 9 + 63) / 64;
+    // ADRS_c prefix and the padding after m values (the length counts the
+    // 64-byte midstate block)
+    SPX_DEV static void frame(uint32_t *stream, const uint32_t *, const Adrs &a, int m, uint32_t lane) {
+        const int end = 22 + m * N;   // = 2 (mod 4)
+        const int nb = stream_blocks(m);
         if (lane < 5) stream[lane] = __byte_perm(a.w[lane], 0, 0x0123);
         if (lane == 5) put16(stream, 20, __byte_perm(a.w[5], 0, 0x0023));
         if (lane == 6) put16(stream, end, 0x80u);
-        for (int q = (end + 2) / 4 + lane; q < nb * 16 - 2; q += 32) stream[q] = 0;
+        for (int q = (end + 2) / 4 + (int)lane; q < nb * 16 - 2; q += 32) stream[q] = 0;
         if (lane == 7) {
             const uint64_t bits = (uint64_t)(64 + end) * 8;
             stream[nb * 16 - 2] = __byte_perm((uint32_t)(bits >> 32), 0, 0x0123);
             stream[nb * 16 - 1] = __byte_perm((uint32_t)bits, 0, 0x0123);
         }
     }
+    SPX_DEV static void load_key(uint32_t *S, const SignWork *wk, const uint8_t *, uint32_t lane) {
+        if (lane < 8) S[B::S_KEY + lane] = wk->mid[lane];
+    }
 
-    // H block(s): ADRS_c || l || r || pad, total length 64 + 22 + 2n bytes
-    SPX_DEV static void h_blocks(uint32_t m[16 * kHBlocks], const Adrs &a, const uint32_t l[W], const uint32_t r[W]) {
-        constexpr int TOT = 22 + 2 * N;
+    SPX_DEV static void claim_chain(LaneRegs &r, const uint32_t *S) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) r.kmid[i] = S[B::S_KEY + i];
+    }
+    SPX_DEV static void claim_t(LaneRegs &r, uint32_t *S, int) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) r.kmid[i] = r.tst[i] = S[B::S_KEY + i];
+    }
+
+    SPX_DEV static void build_chain(Unit &u, const LaneRegs &r, const uint32_t *S, int c, int s,
+                                    const uint32_t v[W]) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) u.st[i] = r.kmid[i];
+        u.blk[0] = S[B::S_AW0];
+        u.blk[1] = S[B::S_AW1];
+        u.blk[2] = S[B::S_AW2];
+        u.blk[3] = S[B::S_IDXL] << 16;
+        u.blk[4] = (uint32_t)c << 16;
+        u.blk[5] = ((uint32_t)s << 16) | (v[0] >> 16);
+#pragma unroll
+        for (int i = 1; i < W; i++) u.blk[5 + i] = __funnelshift_l(v[i], v[i - 1], 16);
+        u.blk[5 + W] = (v[W - 1] << 16) | 0x8000u;
+#pragma unroll
+        for (int i = 6 + W; i < 15; i++) u.blk[i] = 0;
+        u.blk[15] = (64 + 22 + N) * 8;
+    }
+    SPX_DEV static void build_t(Unit &u, const LaneRegs &r, uint32_t *S, int j, int) {
+        const uint32_t *b = S + B::S_HDR + j * 16;
+#pragma unroll
+        for (int i = 0; i < 8; i++) u.st[i] = r.tst[i];
+#pragma unroll
+        for (int i = 0; i < 16; i++) u.blk[i] = __byte_perm(b[i], 0, 0x0123);
+    }
+    // H of compute_root at height h -> h + 1 for node index idx; sub = block
+    SPX_DEV static void build_h(Unit &u, const LaneRegs &r, const uint32_t *S, int h, int sub, uint32_t idx,
+                                const uint32_t v[W], int) {
+        uint32_t sib[W];
+        const uint32_t *auth = S + B::S_HDR + kStreamWords + h * W;
+#pragma unroll
+        for (int i = 0; i < W; i++) sib[i] = __byte_perm(auth[i], 0, 0x0123);
+        const bool right = idx & 1u;
         uint32_t in[2 * W];
 #pragma unroll
-        for (int i = 0; i < W; i++) { in[i] = l[i]; in[W + i] = r[i]; }
+        for (int i = 0; i < W; i++) {
+            in[i] = right ? sib[i] : v[i];
+            in[W + i] = right ? v[i] : sib[i];
+        }
+        Adrs a;
+        a.w[0] = S[B::S_AW0];
+        a.w[1] = S[B::S_AW1];
+        a.w[2] = (S[B::S_AW2] & 0xff000000u) | (ADDR_HASHTREE << 16);
+        a.w[3] = 0;
+        a.w[4] = 0;
+        a.w[5] = 0;
+        adrs_height(a, h + 1);
+        adrs_index(a, idx >> 1);
+        constexpr int TOT = 22 + 2 * N;
+        uint32_t m[16 * kHBlocks];
 #pragma unroll
         for (int i = 0; i < 5; i++) m[i] = a.w[i];
         m[5] = (a.w[5] & 0xffff0000u) | (in[0] >> 16);
@@ -140,12 +231,187 @@ struct PersistVerify {
 #pragma unroll
         for (int i = 6 + 2 * W; i < 16 * kHBlocks; i++) m[i] = 0;
         m[16 * kHBlocks - 1] = (64 + TOT) * 8;
+        if (kHBlocks == 1 || sub == 0) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) u.st[i] = r.kmid[i];
+#pragma unroll
+            for (int i = 0; i < 16; i++) u.blk[i] = m[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; i++) u.st[i] = r.tst[i];
+#pragma unroll
+            for (int i = 0; i < 16; i++) u.blk[i] = m[16 * (kHBlocks - 1) + i];
+        }
+    }
+    SPX_DEV static void build_idle(Unit &u) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) u.st[i] = 0;
+#pragma unroll
+        for (int i = 0; i < 16; i++) u.blk[i] = 0;
+    }
+    SPX_DEV static void run(Unit &u) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) u.out[i] = u.st[i];
+        sha256_rounds<0, 64>(u.out, u.blk);
+#pragma unroll
+        for (int i = 0; i < 8; i++) u.out[i] += u.st[i];
+    }
+    SPX_DEV static void value_out(const Unit &u, uint32_t v[W]) {
+#pragma unroll
+        for (int i = 0; i < W; i++) v[i] = u.out[i];
+    }
+    SPX_DEV static void after_t(const Unit &u, LaneRegs &r, uint32_t *, int) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) r.tst[i] = u.out[i];
+    }
+    SPX_DEV static void after_h_first(const Unit &u, LaneRegs &r) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) r.tst[i] = u.out[i];
     }
 };
 
+// ---------------------------------------------------------------------------
+// SHAKE-256: stream = PUB_SEED || ADRS (32 B) || values || SHAKE padding,
+// 64-bit lanes in memory order (thash_shake256.cu:15-25 absorbs exactly
+// this); unit = one Keccak-f[1600] with one 17-lane block absorbed.  F and
+// H fit one block for every n; the T sponge state (25 lanes) lives in the
+// slot, so only the T lane touches it.
+// ---------------------------------------------------------------------------
+template <class HF>
+struct VerifyShake : VerifySlot<4 * HF::W, 4 * HF::W + 32, 136> {
+    using B = VerifySlot<4 * HF::W, 4 * HF::W + 32, 136>;
+    static constexpr int W = HF::W, N = 4 * W, NL = N / 8, LEN = 2 * N + 3;
+    static constexpr int kPreLanes = NL + 4;
+    static constexpr int stream_blocks(int m) { return (8 * kPreLanes + m * N) / 136 + 1; }
+    static constexpr int kStreamWords = stream_blocks(LEN) * 34;
+    static constexpr int kHBlocks = 1;
+    static constexpr int kTStateWords = 50;
+    static __host__ __device__ int slot_words(int hp) { return B::S_HDR + kStreamWords + hp * W + kTStateWords; }
+
+    struct Unit {
+        uint64_t A[25];
+    };
+    struct LaneRegs {};
+
+    SPX_DEV static uint64_t *lanes(uint32_t *p) { return reinterpret_cast<uint64_t *>(p); }
+    SPX_DEV static const uint64_t *lanes(const uint32_t *p) { return reinterpret_cast<const uint64_t *>(p); }
+    SPX_DEV static uint64_t *tstate(uint32_t *S, int hp) { return lanes(S + B::S_HDR + kStreamWords + hp * W); }
+
+    SPX_DEV static void write_value(uint32_t *stream, int c, const uint32_t v[W]) {
+        uint32_t *d = stream + 2 * (kPreLanes + c * NL);
+#pragma unroll
+        for (int i = 0; i < W; i++) d[i] = v[i];
+    }
+    SPX_DEV static void read_value(const uint32_t *stream, int c, uint32_t v[W]) {
+        const uint32_t *s = stream + 2 * (kPreLanes + c * NL);
+#pragma unroll
+        for (int i = 0; i < W; i++) v[i] = s[i];
+    }
+    SPX_DEV static void copy_values(uint32_t *stream, const uint8_t *src, int bytes, uint32_t lane) {
+        uint64_t *d = lanes(stream) + kPreLanes;
+        for (int q = lane; q < bytes / 8; q += 32) d[q] = reinterpret_cast<const uint64_t *>(src)[q];
+    }
+    // PUB_SEED and ADRS lanes, then the padding after m values
+    SPX_DEV static void frame(uint32_t *stream, const uint32_t *S, const Adrs &a, int m, uint32_t lane) {
+        uint64_t *L = lanes(stream);
+        uint64_t al[4];
+        adrs_lanes(a, al);
+        if (lane < (uint32_t)NL) L[lane] = lane_of(S[B::S_KEY + 2 * lane], S[B::S_KEY + 2 * lane + 1]);
+        if (lane >= (uint32_t)NL && lane < (uint32_t)kPreLanes) L[lane] = al[lane - NL];
+        const int end = kPreLanes + m * NL;   // first lane after the values
+        const int last = 17 * stream_blocks(m) - 1;
+        for (int q = end + (int)lane; q <= last; q += 32)
+            L[q] = (q == end ? 0x1Full : 0ull) ^ (q == last ? 0x8000000000000000ull : 0ull);
+    }
+    SPX_DEV static void load_key(uint32_t *S, const SignWork *, const uint8_t *pk, uint32_t lane) {
+        if (lane < (uint32_t)W) S[B::S_KEY + lane] = reinterpret_cast<const uint32_t *>(pk)[lane];
+    }
+
+    SPX_DEV static void claim_chain(LaneRegs &, const uint32_t *) {}
+    SPX_DEV static void claim_t(LaneRegs &, uint32_t *S, int hp) {
+        uint64_t *T = tstate(S, hp);
+#pragma unroll
+        for (int i = 0; i < 25; i++) T[i] = 0;
+    }
+
+    // PUB_SEED || ADRS (ADRS given as its six big-endian words) into lanes 0..NL+3
+    SPX_DEV static void put_prefix(Unit &u, const uint32_t *S, const uint32_t aw[6]) {
+#pragma unroll
+        for (int i = 0; i < NL; i++) u.A[i] = lane_of(S[B::S_KEY + 2 * i], S[B::S_KEY + 2 * i + 1]);
+        u.A[NL] = lane_of(bswap32(aw[0]), bswap32(aw[1]));
+        u.A[NL + 1] = lane_of(bswap32(aw[2]), bswap32(aw[3]));
+        u.A[NL + 2] = lane_of(bswap32(aw[4]), bswap32(aw[5]));
+        u.A[NL + 3] = 0;
+    }
+    SPX_DEV static void build_chain(Unit &u, const LaneRegs &, const uint32_t *S, int c, int s,
+                                    const uint32_t v[W]) {
+#pragma unroll
+        for (int i = 0; i < 25; i++) u.A[i] = 0;
+        const uint32_t aw[6] = {S[B::S_AW0], S[B::S_AW1], S[B::S_AW2], S[B::S_IDXL] << 16, (uint32_t)c << 16,
+                                (uint32_t)s << 16};
+        put_prefix(u, S, aw);
+#pragma unroll
+        for (int i = 0; i < NL; i++) u.A[kPreLanes + i] = lane_of(v[2 * i], v[2 * i + 1]);
+        u.A[kPreLanes + NL] = 0x1Full;
+        u.A[16] ^= 0x8000000000000000ull;
+    }
+    SPX_DEV static void build_t(Unit &u, const LaneRegs &, uint32_t *S, int j, int hp) {
+        const uint64_t *T = tstate(S, hp);
+        const uint64_t *b = lanes(S + B::S_HDR) + 17 * j;
+#pragma unroll
+        for (int i = 0; i < 17; i++) u.A[i] = T[i] ^ b[i];
+#pragma unroll
+        for (int i = 17; i < 25; i++) u.A[i] = T[i];
+    }
+    SPX_DEV static void build_h(Unit &u, const LaneRegs &, const uint32_t *S, int h, int, uint32_t idx,
+                                const uint32_t v[W], int) {
+        const uint32_t *auth = S + B::S_HDR + kStreamWords + h * W;
+        const bool right = idx & 1u;
+        Adrs a;
+        a.w[0] = S[B::S_AW0];
+        a.w[1] = S[B::S_AW1];
+        a.w[2] = (S[B::S_AW2] & 0xff000000u) | (ADDR_HASHTREE << 16);
+        a.w[3] = 0;
+        a.w[4] = 0;
+        a.w[5] = 0;
+        adrs_height(a, h + 1);
+        adrs_index(a, idx >> 1);
+#pragma unroll
+        for (int i = 0; i < 25; i++) u.A[i] = 0;
+        put_prefix(u, S, a.w);
+#pragma unroll
+        for (int i = 0; i < NL; i++) {
+            const uint64_t sl = lane_of(auth[2 * i], auth[2 * i + 1]);
+            const uint64_t vl = lane_of(v[2 * i], v[2 * i + 1]);
+            u.A[kPreLanes + i] = right ? sl : vl;
+            u.A[kPreLanes + NL + i] = right ? vl : sl;
+        }
+        u.A[kPreLanes + 2 * NL] ^= 0x1Full;
+        u.A[16] ^= 0x8000000000000000ull;
+    }
+    SPX_DEV static void build_idle(Unit &u) {
+#pragma unroll
+        for (int i = 0; i < 25; i++) u.A[i] = 0;
+    }
+    SPX_DEV static void run(Unit &u) { keccak_f1600(u.A); }
+    SPX_DEV static void value_out(const Unit &u, uint32_t v[W]) {
+#pragma unroll
+        for (int i = 0; i < NL; i++) { v[2 * i] = (uint32_t)u.A[i]; v[2 * i + 1] = (uint32_t)(u.A[i] >> 32); }
+    }
+    SPX_DEV static void after_t(const Unit &u, LaneRegs &, uint32_t *S, int hp) {
+        uint64_t *T = tstate(S, hp);
+#pragma unroll
+        for (int i = 0; i < 25; i++) T[i] = u.A[i];
+    }
+    SPX_DEV static void after_h_first(const Unit &, LaneRegs &) {}
+};
+
+template <class HF>
+using VerifyPolicy = typename std::conditional<HF::kShake != 0, VerifyShake<HF>, VerifySha2<HF>>::type;
+
 template <class HF>
 __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A, uint32_t *ctr, int G) {
-    using PV = PersistVerify<HF>;
+    using PV = VerifyPolicy<HF>;
     constexpr int W = PV::W, N = PV::N, LEN = PV::LEN;
     extern __shared__ uint32_t smem[];
     const uint32_t lane = threadIdx.x & 31;
@@ -162,12 +428,9 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
     int ts = 0;                      // chain step / H sub-block
     uint32_t tidx = 0;               // compute_root node index
     uint32_t v[W];                   // chain value / current node
-    uint32_t tst[8];                 // T running state / H first-block state
-    uint32_t kmid[8];                // the task's key midstate (PUB_SEED block)
 #pragma unroll
     for (int i = 0; i < W; i++) v[i] = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) tst[i] = kmid[i] = 0;
+    typename PV::LaneRegs lr{};
     bool upkeep = true;   // a slot may be empty or waiting for its next layer
 
     while (true) {
@@ -193,7 +456,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 }
                 const uint64_t tree = wk->tree;
                 const uint32_t idx_leaf = wk->idx_leaf;
-                if (lane < 8) S[PV::S_MID + lane] = wk->mid[lane];
+                PV::load_key(S, wk, A.pk.row(it), lane);
                 // T_k over the FORS roots (fors.cu:141-142)
                 Adrs pa;
                 adrs_zero(pa);
@@ -201,7 +464,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 adrs_keypair(pa, idx_leaf);
                 adrs_type(pa, ADDR_FORSPK);
                 __syncwarp();
-                PV::stream_frame(stream, pa, P.k, lane);
+                PV::frame(stream, S, pa, P.k, lane);
                 PV::copy_values(stream, A.fors_roots + (uint64_t)it * P.k * N, P.k * N, lane);
                 __syncwarp();
                 if (lane == 0) {
@@ -237,7 +500,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 adrs_tree(pa, tree_L);
                 adrs_keypair(pa, idx_L);
                 adrs_type(pa, ADDR_WOTSPK);
-                PV::stream_frame(stream, pa, LEN, lane);
+                PV::frame(stream, S, pa, LEN, lane);
                 const uint8_t *sl = A.sig + (uint64_t)it * A.sig_stride + N + P.fors_bytes +
                                     (uint64_t)L * (P.wots_bytes + P.hp * N);
                 PV::copy_values(stream, sl, LEN * N, lane);
@@ -283,8 +546,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                     kind = PV::K_T;
                     tg = g;
                     tc = 0;
-#pragma unroll
-                    for (int i = 0; i < 8; i++) kmid[i] = tst[i] = S[PV::S_MID + i];
+                    PV::claim_t(lr, S, P.hp);
                 }
                 __syncwarp();
                 if (lane == 0) S[PV::S_TCLAIM] = 1;
@@ -307,9 +569,8 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                         tg = g;
                         tc = c;
                         ts = s0;
-                        PV::read_value(S + PV::S_HDR, 22 + c * N, v);
-#pragma unroll
-                        for (int i = 0; i < 8; i++) kmid[i] = S[PV::S_MID + i];
+                        PV::read_value(S + PV::S_HDR, c, v);
+                        PV::claim_chain(lr, S);
                     }
                 }
                 const int taken = min(__popc(need), LEN - next);
@@ -321,96 +582,39 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         }
         if (!__any_sync(0xffffffffu, kind != PV::K_NONE)) break;
 
-        // ---- build (state, block) for this lane's compression ----
+        // ---- build this lane's unit of the hash ----
         uint32_t *S = slots + tg * SW;
         bool run = kind != PV::K_NONE;
-        uint32_t st[8], blk[16];
-#pragma unroll
-        for (int i = 0; i < 8; i++) st[i] = kmid[i];
+        typename PV::Unit u;
         if (kind == PV::K_CHAIN) {
-            blk[0] = S[PV::S_AW0];
-            blk[1] = S[PV::S_AW1];
-            blk[2] = S[PV::S_AW2];
-            blk[3] = S[PV::S_IDXL] << 16;
-            blk[4] = (uint32_t)tc << 16;
-            blk[5] = ((uint32_t)ts << 16) | (v[0] >> 16);
-#pragma unroll
-            for (int i = 1; i < W; i++) blk[5 + i] = __funnelshift_l(v[i], v[i - 1], 16);
-            blk[5 + W] = (v[W - 1] << 16) | 0x8000u;
-#pragma unroll
-            for (int i = 6 + W; i < 15; i++) blk[i] = 0;
-            blk[15] = (64 + 22 + N) * 8;
+            PV::build_chain(u, lr, S, tc, ts, v);
         } else if (kind == PV::K_T) {
             // idle while the chains this block covers are still running
             run = PV::done_prefix(S) > PV::block_last_value(tc, (int)S[PV::S_M]);
-            const uint32_t *b = S + PV::S_HDR + tc * 16;
-#pragma unroll
-            for (int i = 0; i < 8; i++) st[i] = tst[i];
-#pragma unroll
-            for (int i = 0; i < 16; i++) blk[i] = __byte_perm(b[i], 0, 0x0123);
+            PV::build_t(u, lr, S, tc, P.hp);
         } else if (kind == PV::K_ROOT) {
-            const int h = tc;   // compute_root step: node at height h -> h + 1
-            uint32_t sib[W];
-            const uint32_t *auth = S + PV::S_HDR + PV::kStreamWords + h * W;
-#pragma unroll
-            for (int i = 0; i < W; i++) sib[i] = __byte_perm(auth[i], 0, 0x0123);
-            const bool right = tidx & 1u;
-            uint32_t l[W], r[W];
-#pragma unroll
-            for (int i = 0; i < W; i++) {
-                l[i] = right ? sib[i] : v[i];
-                r[i] = right ? v[i] : sib[i];
-            }
-            Adrs ta;
-            ta.w[0] = S[PV::S_AW0];
-            ta.w[1] = S[PV::S_AW1];
-            ta.w[2] = (S[PV::S_AW2] & 0xff000000u) | (ADDR_HASHTREE << 16);
-            ta.w[3] = 0;
-            ta.w[4] = 0;
-            ta.w[5] = 0;
-            adrs_height(ta, h + 1);
-            adrs_index(ta, tidx >> 1);
-            uint32_t m[16 * PV::kHBlocks];
-            PV::h_blocks(m, ta, l, r);
-            if (PV::kHBlocks == 1 || ts == 0) {
-#pragma unroll
-                for (int i = 0; i < 16; i++) blk[i] = m[i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < 8; i++) st[i] = tst[i];
-#pragma unroll
-                for (int i = 0; i < 16; i++) blk[i] = m[16 * (PV::kHBlocks - 1) + i];
-            }
+            PV::build_h(u, lr, S, tc, ts, tidx, v, P.hp);
         } else {
-#pragma unroll
-            for (int i = 0; i < 16; i++) blk[i] = 0;
+            PV::build_idle(u);
         }
 
-        // ---- one compression, converged across the warp ----
-        uint32_t t[8];
-#pragma unroll
-        for (int i = 0; i < 8; i++) t[i] = st[i];
-        sha256_rounds<0, 64>(t, blk);
-#pragma unroll
-        for (int i = 0; i < 8; i++) t[i] += st[i];
+        // ---- one unit of the hash, converged across the warp ----
+        PV::run(u);
 
         // ---- use the output ----
         bool slot_event = false;
         if (run && kind == PV::K_CHAIN) {
-#pragma unroll
-            for (int i = 0; i < W; i++) v[i] = t[i];
+            PV::value_out(u, v);
             if (++ts >= 15) {
-                PV::write_value(S + PV::S_HDR, 22 + tc * N, v);
+                PV::write_value(S + PV::S_HDR, tc, v);
                 __threadfence_block();   // the end value is in the stream before its done bit
                 PV::mark_done(S, tc);
                 kind = PV::K_NONE;
             }
         } else if (run && kind == PV::K_T) {
-#pragma unroll
-            for (int i = 0; i < 8; i++) tst[i] = t[i];
+            PV::after_t(u, lr, S, P.hp);
             if (++tc >= (int)S[PV::S_NB]) {
-#pragma unroll
-                for (int i = 0; i < W; i++) v[i] = t[i];
+                PV::value_out(u, v);
                 if ((int)S[PV::S_LAYER] < 0) {
                     // FORS public key: the message of layer 0
 #pragma unroll
@@ -427,12 +631,10 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
             }
         } else if (run && kind == PV::K_ROOT) {
             if (PV::kHBlocks == 2 && ts == 0) {
-#pragma unroll
-                for (int i = 0; i < 8; i++) tst[i] = t[i];
+                PV::after_h_first(u, lr);
                 ts = 1;
             } else {
-#pragma unroll
-                for (int i = 0; i < W; i++) v[i] = t[i];
+                PV::value_out(u, v);
                 ts = 0;
                 tidx >>= 1;
                 if (++tc >= P.hp) {

@@ -18,7 +18,7 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 OUT = os.path.dirname(os.path.abspath(__file__))
 SETS = ["sha256-128f", "sha256-192f", "sha256-256f", "shake256-128f", "shake256-192f", "shake256-256f",
-        "sha256-128s", "shake256-128s"]
+        "sha256-128s", "shake256-128s", "sha256-192s", "sha256-256s", "shake256-192s", "shake256-256s"]
 
 
 def parse_rsp(text):

@@ -13,7 +13,8 @@ import pytest
 from conftest import GOLDEN
 
 KAT_SETS = [s for s in ("sha256-128f", "sha256-192f", "sha256-256f", "shake256-128f", "shake256-192f",
-                        "shake256-256f", "sha256-128s", "shake256-128s")
+                        "shake256-256f", "sha256-128s", "shake256-128s", "sha256-192s", "sha256-256s",
+                        "shake256-192s", "shake256-256s")
             if os.path.exists(os.path.join(GOLDEN, "kat_%s.json" % s))]
 
 

@@ -46,6 +46,7 @@ OPS_PER_CMP = 1384   # INT ops of one SHA-256 compression (64 rounds x 14 + 48 x
 # verify = FORS roots + T_k + d x (chains + T_len + auth path)
 SIGN_CMP_128F = 113265
 VERIFY_CMP_128F = 6400
+KEYGEN_CMP_128F = 4567   # top-layer XMSS tree: 8 leaves x 570 + 7 H
 
 
 def int_frac(signs, verifies, peak_ops):
@@ -302,6 +303,9 @@ def main():
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_launch_scaled_to_4096")
 
+    # ---- batched key generation (crypto_sign_seed_keypair per item) ----
+    keygen = keygen_run(c, eng, sid, z, o, flush, args.steps, args.warmup, peak_ops) if rank == 0 else None
+
     # ---- end-to-end through the C ABI with host buffers ----
     e2e_ms = []
     for i in range(args.warmup + args.steps):
@@ -354,6 +358,7 @@ def main():
             "verify": {"value": verify_value, "unit": "verify/s", "ms_per_batch": verify_total / args.steps,
                        "roofline_frac": int_frac(0, verify_value, peak_ops)},
             "step_roofline_frac": int_frac(value, 0, peak_ops),
+            "keygen": keygen,
             "e2e": {"value": e2e_value, "unit": "sign/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_total / args.steps},
             "gpu_launches": (5 + 3) * args.steps,
@@ -389,6 +394,40 @@ def main():
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def keygen_run(c, eng, sid, z, oracle, flush, steps, warmup, peak_ops):
+    """4096 SHA-256-128f keypairs from seeded 48-byte seeds in one
+    graph-launched batch; three are byte-compared with the oracle's
+    crypto_sign_seed_keypair before timing."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(4242)
+    seeds = rng.integers(0, 256, size=(BATCH, z["seed"]), dtype=np.uint8)
+    kb = eng.batch(c.OP_KEYGEN, sid, BATCH)
+    kb.upload(BATCH, np.ascontiguousarray(seeds.reshape(-1)))
+    kb.run()
+    sk = np.zeros(BATCH * z["sk"], dtype=np.uint8)
+    pk = np.zeros(BATCH * z["pk"], dtype=np.uint8)
+    kb.download(sk, pk)
+    for i in (0, 1, BATCH - 1):
+        rpk, rsk = oracle.seed_keypair(bytes(seeds[i]))
+        assert bytes(sk[i * z["sk"]:(i + 1) * z["sk"]]) == rsk, "keypair %d differs from the CPU oracle" % i
+        assert bytes(pk[i * z["pk"]:(i + 1) * z["pk"]]) == rpk, "keypair %d differs from the CPU oracle" % i
+    for _ in range(warmup):
+        kb.run()
+    kb.sync()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        kb.run(); kb.sync(); ms.append(kb.last_ms())
+    kb.close()
+    tot = sum(ms)
+    v = BATCH * steps / (tot / 1e3)
+    return {"value": v, "unit": "keypair/s", "ms_per_batch": tot / steps, "batch": BATCH,
+            "subset_check": "3 keypairs byte-identical to the CPU oracle",
+            "roofline_frac": v * KEYGEN_CMP_128F * OPS_PER_CMP / peak_ops}
 
 
 def served_runs(c, eng, peak_ops, seconds=2.0):

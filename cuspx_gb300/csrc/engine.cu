@@ -80,6 +80,9 @@ using namespace cuspx;
 // items per batch for which chain-parallel leaf scratch is allocated (the
 // largest chain_mode_max that can take effect)
 static const size_t kChainModeItems = 256;
+// messages of at least this many bytes (32 SHA-256 blocks) are hashed by the
+// two-warp message kernels of the SHA-256 sets
+static const uint64_t kPairMsgBytes = 2048;
 
 struct cuspx_ctx {
     int device = 0;
@@ -93,6 +96,7 @@ struct cuspx_ctx {
     struct GroupGraph {
         std::vector<cuspx_batch *> batches;
         std::vector<size_t> counts;
+        std::vector<bool> long_msgs;
         std::vector<Tuning> tunes;
         cudaGraphExec_t exec;
         cudaStream_t origin;
@@ -126,6 +130,9 @@ struct cuspx_batch {
     uint8_t *fors_roots = nullptr, *leaves = nullptr, *roots = nullptr, *chains = nullptr;
     uint8_t *wpk = nullptr, *cur_root = nullptr;
     uint32_t *ctr = nullptr;   // persistent verify item counter
+    bool long_msgs = false;    // the last upload held a message of >= kPairMsgBytes (SHA-256:
+                               // hash those over two warps; both kernels read the device
+                               // lengths, so the split is right whatever the flag says)
     uint8_t *ends = nullptr;   // chain-parallel leaf scratch
     uint32_t ends_cap = 0;
     size_t count = 0;
@@ -137,12 +144,12 @@ struct cuspx_batch {
     // its second use
     struct GraphKey {
         size_t count;
-        bool keyrow, aux, siglen;
+        bool keyrow, aux, siglen, long_msgs;
         const uint8_t *keys;
         Tuning tune;
         bool operator==(const GraphKey &o) const {
-            return count == o.count && keyrow == o.keyrow && aux == o.aux && siglen == o.siglen && keys == o.keys &&
-                   memcmp(&tune, &o.tune, sizeof(Tuning)) == 0;
+            return count == o.count && keyrow == o.keyrow && aux == o.aux && siglen == o.siglen &&
+                   long_msgs == o.long_msgs && keys == o.keys && memcmp(&tune, &o.tune, sizeof(Tuning)) == 0;
         }
     };
     struct GraphEntry {
@@ -469,6 +476,8 @@ int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t
         CK(cudaMemcpyAsync(b->off, msg_off, count * 8, cudaMemcpyHostToDevice, b->s), ctx);
         CK(cudaMemcpyAsync(b->len, msg_len, count * 8, cudaMemcpyHostToDevice, b->s), ctx);
     }
+    b->long_msgs = false;
+    for (size_t i = 0; i < count && !b->long_msgs; i++) b->long_msgs = msg_len[i] >= kPairMsgBytes;
     b->use_keyrow = key_index != nullptr;
     if (b->op == CUSPX_OP_SIGN) {
         b->use_aux = aux != nullptr;
@@ -504,6 +513,7 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.status = b->status;
         A.ends = b->ends;
         A.ends_cap = b->ends_cap;
+        A.long_msg = b->long_msgs ? kPairMsgBytes : 0;
         ops.sign(P, A, tu, b->s, pt);
     } else if (b->op == CUSPX_OP_VERIFY) {
         VerifyArgs A;
@@ -520,6 +530,7 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.wpk = b->wpk;
         A.cur_root = b->cur_root;
         A.ctr = b->ctr;
+        A.long_msg = b->long_msgs ? kPairMsgBytes : 0;
         ops.verify(P, A, tu, b->s, pt);
     } else {
         KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots, b->ends, b->ends_cap};
@@ -561,7 +572,7 @@ int cuspx_batch_run(cuspx_batch *b) {
         return CUSPX_OK;
     }
     const Tuning &tu = ctx->tune[b->set];
-    cuspx_batch::GraphKey key{b->count, b->use_keyrow, b->use_aux, b->use_siglen, b->bound_keys, tu};
+    cuspx_batch::GraphKey key{b->count, b->use_keyrow, b->use_aux, b->use_siglen, b->long_msgs, b->bound_keys, tu};
     b->use_clock++;
     cuspx_batch::GraphEntry *hit = nullptr;
     for (auto &g : b->graphs)
@@ -822,7 +833,7 @@ int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *
         bool same = true;
         for (int i = 0; i < nb && same; i++) {
             cuspx_batch *b = batches[i];
-            same = g.batches[i] == b && g.counts[i] == b->count &&
+            same = g.batches[i] == b && g.counts[i] == b->count && g.long_msgs[i] == b->long_msgs &&
                    memcmp(&g.tunes[i], &ctx->tune[b->set], sizeof(Tuning)) == 0;
         }
         if (same) hit = &g;
@@ -832,6 +843,7 @@ int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *
         gg.batches.assign(batches, batches + nb);
         for (int i = 0; i < nb; i++) {
             gg.counts.push_back(batches[i]->count);
+            gg.long_msgs.push_back(batches[i]->long_msgs);
             gg.tunes.push_back(ctx->tune[batches[i]->set]);
         }
         CK(cudaStreamCreateWithFlags(&gg.origin, cudaStreamNonBlocking), ctx);

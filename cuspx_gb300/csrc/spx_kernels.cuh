@@ -82,6 +82,8 @@ struct SignArgs {
     int32_t *status;           // count
     uint8_t *ends = nullptr;   // chain-parallel scratch: ends_cap x d x 2^hp x len x n, or null
     uint32_t ends_cap = 0;
+    uint64_t long_msg = 0;     // messages of at least this many bytes are hashed by
+                               // k_sign_msg_pair instead of k_sign_msg (0: none)
 };
 
 // tree/leaf indices of hypertree layer L (sign.cu:1987-1988)
@@ -128,6 +130,29 @@ SPX_DEV uint32_t chain_len(const SetParams &P, const uint32_t msg[HF::W], int c)
     return (csum >> (cbits - 4 * (j + 1))) & 15u;
 }
 
+// Work record of an item from its H_msg digest (hash_sha256.cu:249-261):
+// FORS digest, tree and leaf index, and the key's midstate from PUB_SEED.
+template <class HF>
+SPX_DEV SignWork work_from_digest(const SetParams &P, const uint8_t *dg, const uint8_t *pub) {
+    constexpr int N = 4 * HF::W;
+    SignWork w;
+    for (int j = 0; j < 48; j++) w.mhash[j] = j < P.fors_msg_bytes ? dg[j] : 0;
+    uint64_t t = 0;
+    for (int j = 0; j < P.tree_bytes; j++) t = (t << 8) | dg[P.fors_msg_bytes + j];
+    if (P.tree_bits < 64) t &= (~0ull) >> (64 - P.tree_bits);
+    uint32_t l = 0;
+    for (int j = 0; j < P.leaf_bytes; j++) l = (l << 8) | dg[P.fors_msg_bytes + P.tree_bytes + j];
+    l &= (~0u) >> (32 - P.leaf_bits);
+    w.tree = t;
+    w.idx_leaf = l;
+    w.flags = 0;
+    KeyRegs<N> key;
+    HF::key_init(key, pub, pub);
+#pragma unroll
+    for (int j = 0; j < 8; j++) w.mid[j] = key.mid[j];
+    return w;
+}
+
 // ===========================================================================
 // message phase: thread per signature
 // ===========================================================================
@@ -149,27 +174,60 @@ __global__ void k_sign_msg(SetParams P, SignArgs A) {
     }
     const uint8_t *m = A.msg.base + A.msg.off[i];
     const uint64_t mlen = A.msg.len[i];
+    if (A.long_msg && mlen >= A.long_msg) return;   // k_sign_msg_pair hashes it
     HF::prf_msg(R, skprf, opt, m, mlen);
     uint8_t *sig = A.sig + (uint64_t)i * P.sig_bytes;
     HF::store(sig, R);
     uint8_t dg[64];
     HF::h_msg(dg, P.dgst_bytes, R, pk, m, mlen);
-    SignWork w;
-    for (int j = 0; j < 48; j++) w.mhash[j] = j < P.fors_msg_bytes ? dg[j] : 0;
-    uint64_t t = 0;
-    for (int j = 0; j < P.tree_bytes; j++) t = (t << 8) | dg[P.fors_msg_bytes + j];
-    if (P.tree_bits < 64) t &= (~0ull) >> (64 - P.tree_bits);
-    uint32_t l = 0;
-    for (int j = 0; j < P.leaf_bytes; j++) l = (l << 8) | dg[P.fors_msg_bytes + P.tree_bytes + j];
-    l &= (~0u) >> (32 - P.leaf_bits);
-    w.tree = t;
-    w.idx_leaf = l;
-    w.flags = 0;
-    KeyRegs<N> key;
-    HF::key_init(key, sk, sk + 2 * N);
+    A.work[i] = work_from_digest<HF>(P, dg, sk + 2 * N);
+}
+
+// Two warps per signature for long messages (SHA-256 sets): the same
+// PRF_msg and H_msg as k_sign_msg, each message pass split into a
+// schedule-building warp and a rounds warp (Sha2::stream_msg_pair).  Blocks
+// whose message is shorter than long_msg return at once.
+template <class HF>
+__global__ void __launch_bounds__(64) k_sign_msg_pair(SetParams P, SignArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    __shared__ uint32_t kw[128];
+    __shared__ uint32_t xr[8];
+    const uint32_t i = blockIdx.x;
+    if (i >= A.count || A.msg.len[i] < A.long_msg) return;   // uniform over the block
+    const int role = threadIdx.x == 0 ? 0 : (threadIdx.x == 32 ? 1 : 2);
+    const uint8_t *sk = A.sk.row(i);
+    uint32_t skprf[W], opt[W], pre[3 * W];
+    HF::load(skprf, sk + N);
+    if (A.optrand) {
+        HF::load(opt, A.optrand + (uint64_t)i * N);
+    } else {
 #pragma unroll
-    for (int j = 0; j < 8; j++) w.mid[j] = key.mid[j];
-    A.work[i] = w;
+        for (int j = 0; j < W; j++) opt[j] = 0xadadadadu;
+    }
+    const uint8_t *m = A.msg.base + A.msg.off[i];
+    const uint64_t mlen = A.msg.len[i];
+    uint32_t st[8];
+    if (role == 1) HF::hmac_start(st, skprf);
+    HF::template stream_msg_pair<W>(st, 1, opt, m, mlen, kw, role);
+    if (role == 1) {
+        uint32_t R[W];
+        HF::hmac_finish(R, st, skprf);
+        HF::store(A.sig + (uint64_t)i * P.sig_bytes, R);
+#pragma unroll
+        for (int j = 0; j < W; j++) xr[j] = R[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < W; j++) pre[j] = xr[j];
+    HF::load(pre + W, sk + 2 * N);
+    HF::load(pre + 2 * W, sk + 3 * N);
+    if (role == 1) sha256_iv(st);
+    HF::template stream_msg_pair<3 * W>(st, 0, pre, m, mlen, kw, role);
+    if (role == 1) {
+        uint8_t dg[64];
+        HF::mgf1_digest(dg, P.dgst_bytes, st);
+        A.work[i] = work_from_digest<HF>(P, dg, sk + 2 * N);
+    }
 }
 
 // ===========================================================================
@@ -667,6 +725,7 @@ struct VerifyArgs {
     uint8_t *wpk;               // count x len x n: WOTS public key of the current layer
     uint8_t *cur_root;          // count x n: root of the layer below (FORS key for layer 0)
     uint32_t *ctr = nullptr;    // persistent verify: next item to take (zeroed per launch)
+    uint64_t long_msg = 0;      // as SignArgs::long_msg, for k_verify_msg_pair
 };
 
 template <class HF>
@@ -684,6 +743,7 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A) {
         A.work[i] = w;
         return;
     }
+    if (A.long_msg && A.msg.len[i] >= A.long_msg) return;   // k_verify_msg_pair hashes it
     const uint8_t *pkb = A.pk.row(i);
     const uint8_t *sig = A.sig + (uint64_t)i * A.sig_stride;
     uint32_t R[W], pk[2 * W];
@@ -692,20 +752,31 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A) {
     HF::load(pk + W, pkb + N);
     uint8_t dg[64];
     HF::h_msg(dg, P.dgst_bytes, R, pk, A.msg.base + A.msg.off[i], A.msg.len[i]);
-    for (int j = 0; j < 48; j++) w.mhash[j] = j < P.fors_msg_bytes ? dg[j] : 0;
-    uint64_t t = 0;
-    for (int j = 0; j < P.tree_bytes; j++) t = (t << 8) | dg[P.fors_msg_bytes + j];
-    if (P.tree_bits < 64) t &= (~0ull) >> (64 - P.tree_bits);
-    uint32_t l = 0;
-    for (int j = 0; j < P.leaf_bytes; j++) l = (l << 8) | dg[P.fors_msg_bytes + P.tree_bytes + j];
-    l &= (~0u) >> (32 - P.leaf_bits);
-    w.tree = t;
-    w.idx_leaf = l;
-    KeyRegs<N> key;
-    HF::key_init(key, pkb, pkb);
-#pragma unroll
-    for (int j = 0; j < 8; j++) w.mid[j] = key.mid[j];
-    A.work[i] = w;
+    A.work[i] = work_from_digest<HF>(P, dg, pkb);
+}
+
+// H_msg of long messages over two warps (SHA-256 sets), as k_sign_msg_pair
+template <class HF>
+__global__ void __launch_bounds__(64) k_verify_msg_pair(SetParams P, VerifyArgs A) {
+    constexpr int W = HF::W, N = 4 * W;
+    __shared__ uint32_t kw[128];
+    const uint32_t i = blockIdx.x;
+    if (i >= A.count || A.msg.len[i] < A.long_msg) return;   // uniform over the block
+    if (A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes) return;   // k_verify_msg rejected it
+    const int role = threadIdx.x == 0 ? 0 : (threadIdx.x == 32 ? 1 : 2);
+    const uint8_t *pkb = A.pk.row(i);
+    uint32_t pre[3 * W];
+    HF::load(pre, A.sig + (uint64_t)i * A.sig_stride);
+    HF::load(pre + W, pkb);
+    HF::load(pre + 2 * W, pkb + N);
+    uint32_t st[8];
+    if (role == 1) sha256_iv(st);
+    HF::template stream_msg_pair<3 * W>(st, 0, pre, A.msg.base + A.msg.off[i], A.msg.len[i], kw, role);
+    if (role == 1) {
+        uint8_t dg[64];
+        HF::mgf1_digest(dg, P.dgst_bytes, st);
+        A.work[i] = work_from_digest<HF>(P, dg, pkb);
+    }
 }
 
 // root from a leaf and its auth path (compute_root, utils.cu:94-135)

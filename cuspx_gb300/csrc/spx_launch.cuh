@@ -169,10 +169,18 @@ struct Family {
         CUSPX_MARK(pt, "k_leaves", s);
     }
 
-    static void sign(const SetParams &P, const SignArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
-        if (A.count == 0) return;
+    static void sign(const SetParams &P, const SignArgs &A0, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
+        if (A0.count == 0) return;
+        SignArgs A = A0;
+        if (HF::kShake) A.long_msg = 0;   // the two-warp message kernels are SHA-256 only
         k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_sign_msg", s);
+        if constexpr (!HF::kShake) {
+            if (A.long_msg) {
+                k_sign_msg_pair<HF><<<A.count, 64, 0, s>>>(P, A);
+                CUSPX_MARK(pt, "k_sign_msg_pair", s);
+            }
+        }
         {
             const int b = tu.fors_block;
             // small batches: spread each tree over more lanes until the launch
@@ -196,10 +204,18 @@ struct Family {
         CUSPX_MARK(pt, "k_sign_finish", s);
     }
 
-    static void verify(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
-        if (A.count == 0) return;
+    static void verify(const SetParams &P, const VerifyArgs &A0, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
+        if (A0.count == 0) return;
+        VerifyArgs A = A0;
+        if (HF::kShake) A.long_msg = 0;
         k_verify_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_verify_msg", s);
+        if constexpr (!HF::kShake) {
+            if (A.long_msg) {
+                k_verify_msg_pair<HF><<<A.count, 64, 0, s>>>(P, A);
+                CUSPX_MARK(pt, "k_verify_msg_pair", s);
+            }
+        }
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_verify_fors", s);
         const int b = tu.verify_block;

@@ -380,62 +380,99 @@ struct Sha2 {
             for (int i = 0; i < 16; i++) w[i] = bswap32(reinterpret_cast<const uint32_t *>(p)[i]);
         }
     }
+    // Block b of prefix (P words, registers) || m || SHA-256 padding, where
+    // bits is the total message length in bits.  Blocks wholly inside the
+    // message come from the one-block-ahead vector load in nxt (have), and
+    // block b + 1 is loaded into nxt here when it is such a block.
+    template <int P>
+    SPX_DEV static void next_block(uint32_t w[16], uint64_t b, uint64_t nblocks, uint64_t bits, const uint32_t pre[P],
+                                   const uint8_t *m, uint64_t mlen, uint32_t nxt[16], bool &have) {
+        constexpr int PB = (P + 15) / 16;  // blocks that contain prefix words
+        auto full = [&](uint64_t x) { return x >= (uint64_t)PB && 4 * (16 * x - P + 16) <= mlen; };
+        if (have) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) w[j] = nxt[j];
+        } else if (b < PB) {
+#pragma unroll
+            for (int pb = 0; pb < PB; pb++) {
+                if (pb == (int)b) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int g = 16 * pb + j;
+                        w[j] = g < P ? pre[g < P ? g : 0] : msg_word(m, mlen, (uint64_t)(g - P));
+                    }
+                }
+            }
+        } else {
+            const uint64_t q0 = 16 * b - P;
+#pragma unroll
+            for (int j = 0; j < 16; j++) w[j] = msg_word(m, mlen, q0 + j);
+        }
+        have = b + 1 < nblocks && full(b + 1);
+        if (have) msg_block_full<P>(nxt, m, 16 * (b + 1) - P);
+        if (b == nblocks - 1) {
+            w[14] = (uint32_t)(bits >> 32);
+            w[15] = (uint32_t)bits;
+        }
+    }
+
     // absorb prefix (P words, registers) || m into st, which has already
-    // absorbed pre_blocks 64-byte blocks; out = final state.  Blocks wholly
-    // inside the message are vector-loaded one block ahead of the compression.
+    // absorbed pre_blocks 64-byte blocks; out = final state.
     template <int P>
     SPX_DEV static void stream_msg(uint32_t st[8], uint32_t pre_blocks, const uint32_t pre[P], const uint8_t *m,
                                    uint64_t mlen) {
         const uint64_t dbytes = 4 * (uint64_t)P + mlen;
         const uint64_t nblocks = (dbytes + 9 + 63) / 64;
         const uint64_t bits = (64 * (uint64_t)pre_blocks + dbytes) * 8;
-        constexpr int PB = (P + 15) / 16;  // blocks that contain prefix words
-        auto full = [&](uint64_t b) { return b >= (uint64_t)PB && 4 * (16 * b - P + 16) <= mlen; };
         uint32_t nxt[16];
         bool have = false;
         for (uint64_t b = 0; b < nblocks; b++) {
             uint32_t w[16];
-            if (have) {
-#pragma unroll
-                for (int j = 0; j < 16; j++) w[j] = nxt[j];
-            } else if (b < PB) {
-#pragma unroll
-                for (int pb = 0; pb < PB; pb++) {
-                    if (pb == (int)b) {
-#pragma unroll
-                        for (int j = 0; j < 16; j++) {
-                            const int g = 16 * pb + j;
-                            w[j] = g < P ? pre[g < P ? g : 0] : msg_word(m, mlen, (uint64_t)(g - P));
-                        }
-                    }
-                }
-            } else {
-                const uint64_t q0 = 16 * b - P;
-#pragma unroll
-                for (int j = 0; j < 16; j++) w[j] = msg_word(m, mlen, q0 + j);
-            }
-            have = b + 1 < nblocks && full(b + 1);
-            if (have) msg_block_full<P>(nxt, m, 16 * (b + 1) - P);
-            if (b == nblocks - 1) {
-                w[14] = (uint32_t)(bits >> 32);
-                w[15] = (uint32_t)bits;
-            }
+            next_block<P>(w, b, nblocks, bits, pre, m, mlen, nxt, have);
             sha256_compress(st, w);
         }
     }
 
-    // PRF_msg = HMAC-SHA256(SK_PRF, optrand || m), truncated (hash_sha256.cu:99-145)
-    SPX_DEV static void prf_msg(uint32_t R[W], const uint32_t skprf[W], const uint32_t optrand[W],
-                                const uint8_t *m, uint64_t mlen) {
-        uint32_t st[8], w[16];
+    // The same absorption split over two warps of a 64-thread block, for long
+    // messages: one thread hashing alone is bound by its own instruction
+    // issue, about 1.3k ALU instructions per block.  Thread 0 (role 0) builds
+    // each block and its schedule with the round constants added into kw (a
+    // shared 2 x 64-word double buffer); thread 32 (role 1) runs the 64 rounds
+    // from kw a block behind; one __syncthreads per block hands a buffer over.
+    // Every thread of the block calls this with the same arguments (other
+    // threads pass role 2 and only take part in the barriers); the result is
+    // in role 1's st.
+    template <int P>
+    SPX_DEV static void stream_msg_pair(uint32_t st[8], uint32_t pre_blocks, const uint32_t pre[P],
+                                        const uint8_t *m, uint64_t mlen, uint32_t *kw, int role) {
+        const uint64_t dbytes = 4 * (uint64_t)P + mlen;
+        const uint64_t nblocks = (dbytes + 9 + 63) / 64;
+        const uint64_t bits = (64 * (uint64_t)pre_blocks + dbytes) * 8;
+        uint32_t nxt[16];
+        bool have = false;
+        for (uint64_t b = 0; b <= nblocks; b++) {
+            if (role == 0 && b < nblocks) {
+                uint32_t w[16];
+                next_block<P>(w, b, nblocks, bits, pre, m, mlen, nxt, have);
+                sha256_schedule_kw(kw + 64 * (b & 1), w);
+            }
+            if (role == 1 && b >= 1) sha256_compress_kw(st, kw + 64 * ((b - 1) & 1));
+            __syncthreads();
+        }
+    }
+
+    // PRF_msg = HMAC-SHA256(SK_PRF, optrand || m), truncated (hash_sha256.cu:99-145):
+    // the inner hash starts from the key block xor ipad, the outer one hashes
+    // the key block xor opad and the inner digest
+    SPX_DEV static void hmac_start(uint32_t st[8], const uint32_t skprf[W]) {
+        uint32_t w[16];
         sha256_iv(st);
 #pragma unroll
         for (int i = 0; i < 16; i++) w[i] = (i < W ? skprf[i] : 0u) ^ 0x36363636u;
         sha256_compress(st, w);
-        stream_msg<W>(st, 1, optrand, m, mlen);
-        uint32_t inner[8];
-#pragma unroll
-        for (int i = 0; i < 8; i++) inner[i] = st[i];
+    }
+    SPX_DEV static void hmac_finish(uint32_t R[W], const uint32_t inner[8], const uint32_t skprf[W]) {
+        uint32_t st[8], w[16];
         sha256_iv(st);
 #pragma unroll
         for (int i = 0; i < 16; i++) w[i] = (i < W ? skprf[i] : 0u) ^ 0x5c5c5c5cu;
@@ -450,19 +487,17 @@ struct Sha2 {
 #pragma unroll
         for (int i = 0; i < W; i++) R[i] = st[i];
     }
+    SPX_DEV static void prf_msg(uint32_t R[W], const uint32_t skprf[W], const uint32_t optrand[W],
+                                const uint8_t *m, uint64_t mlen) {
+        uint32_t st[8];
+        hmac_start(st, skprf);
+        stream_msg<W>(st, 1, optrand, m, mlen);
+        hmac_finish(R, st, skprf);
+    }
 
     // H_msg = MGF1-SHA256(SHA256(R || PK || m), dgst) (hash_sha256.cu:200-262);
     // writes dgst_bytes bytes to dg (a byte array in registers/local).
-    SPX_DEV static void h_msg(uint8_t *dg, int dgst_bytes, const uint32_t R[W], const uint32_t pk[2 * W],
-                              const uint8_t *m, uint64_t mlen) {
-        uint32_t pre[3 * W];
-#pragma unroll
-        for (int i = 0; i < W; i++) pre[i] = R[i];
-#pragma unroll
-        for (int i = 0; i < 2 * W; i++) pre[W + i] = pk[i];
-        uint32_t seed[8];
-        sha256_iv(seed);
-        stream_msg<3 * W>(seed, 0, pre, m, mlen);
+    SPX_DEV static void mgf1_digest(uint8_t *dg, int dgst_bytes, const uint32_t seed[8]) {
         for (int c = 0; 32 * c < dgst_bytes; c++) {
             uint32_t w[16], s[8];
 #pragma unroll
@@ -477,6 +512,18 @@ struct Sha2 {
             for (int i = 0; i < 32 && 32 * c + i < dgst_bytes; i++)
                 dg[32 * c + i] = (uint8_t)(s[i >> 2] >> (24 - 8 * (i & 3)));
         }
+    }
+    SPX_DEV static void h_msg(uint8_t *dg, int dgst_bytes, const uint32_t R[W], const uint32_t pk[2 * W],
+                              const uint8_t *m, uint64_t mlen) {
+        uint32_t pre[3 * W];
+#pragma unroll
+        for (int i = 0; i < W; i++) pre[i] = R[i];
+#pragma unroll
+        for (int i = 0; i < 2 * W; i++) pre[W + i] = pk[i];
+        uint32_t seed[8];
+        sha256_iv(seed);
+        stream_msg<3 * W>(seed, 0, pre, m, mlen);
+        mgf1_digest(dg, dgst_bytes, seed);
     }
 };
 

@@ -263,3 +263,31 @@ def test_mixed_sets_one_launch_vs_oracle(engine):
             assert sig == oracles[n].sign(m, sk), n
     finally:
         ms.close()
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "sha256-192f-simple", "sha256-256f-simple"])
+def test_long_messages_two_warp_hashing(engine, setname):
+    """Batches holding messages of 2 KiB and more hash those over two warps
+    per message (schedule warp + rounds warp) and the rest one thread each;
+    signatures and verdicts equal the CPU oracle's on both sides of the
+    threshold, with a corrupted and a wrong-length signature mixed in."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(2048)
+    seed = bytes(rng.randrange(256) for _ in range(3 * o.p.n))
+    pk, sk = o.seed_keypair(seed)
+    lens = [0, 100, 2047, 2048, 2049, 3000, 20000, 64]
+    msgs = [bytes(rng.randrange(256) for _ in range(L)) for L in lens]
+    sigs, st = engine.sign_batch(sid, [sk] * len(msgs), msgs)
+    assert list(st) == [0] * len(msgs)
+    for m, s in zip(msgs, sigs):
+        assert s == o.sign(m, sk), len(m)
+    bad = bytearray(sigs[6])
+    bad[rng.randrange(len(bad))] ^= 0x10
+    vsigs = list(sigs) + [bytes(bad), sigs[4]]
+    vmsgs = msgs + [msgs[6], msgs[4]]
+    siglens = [len(s) for s in vsigs[:-1]] + [len(sigs[4]) - 1]
+    want = [o.verify(s, m, pk) for s, m in zip(vsigs[:-1], vmsgs[:-1])] + [-1]
+    assert want.count(-1) == 2
+    got = engine.verify_batch(sid, [pk] * len(vmsgs), vmsgs, vsigs, siglens=siglens)
+    assert list(got) == want

@@ -142,8 +142,10 @@ SPX_DEV void sha256_rounds(uint32_t st[8], uint32_t w[16]) {
     st[0] = a; st[1] = b; st[2] = c; st[3] = d; st[4] = e; st[5] = f; st[6] = g; st[7] = h;
 }
 
-// Message schedule with the round constants added: kw[t] = W_t + K_t for
-// t = 0..63 from the 16 block words w (consumed).
+// Message schedule with the round constants added: kw[t * S] = W_t + K_t
+// for t = 0..63 from the 16 block words w (consumed); S interleaves the
+// buffers of several threads in shared memory.
+template <int S>
 SPX_DEV void sha256_schedule_kw(uint32_t *kw, uint32_t w[16]) {
 #pragma unroll
     for (int i = 0; i < 64; i++) {
@@ -153,17 +155,18 @@ SPX_DEV void sha256_schedule_kw(uint32_t *kw, uint32_t w[16]) {
             const uint32_t s1 = rotr(y, 17) ^ rotr(y, 19) ^ (y >> 10);
             w[i & 15] = w[i & 15] + s0 + w[(i - 7) & 15] + s1;
         }
-        kw[i] = add_fma(w[i & 15], sha256_k(i));
+        kw[i * S] = add_fma(w[i & 15], sha256_k(i));
     }
 }
 
-// s <- compress(s) with the schedule given as kw[t] = W_t + K_t (the
+// s <- compress(s) with the schedule given as kw[t * S] = W_t + K_t (the
 // rounds alone: the schedule was computed elsewhere)
+template <int S>
 SPX_DEV void sha256_compress_kw(uint32_t s[8], const uint32_t *kw) {
     uint32_t a = s[0], b = s[1], c = s[2], d = s[3], e = s[4], f = s[5], g = s[6], h = s[7];
 #pragma unroll
     for (int i = 0; i < 64; i++) {
-        const uint32_t t1 = add_fma(h, kw[i]) + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g));
+        const uint32_t t1 = add_fma(h, kw[i * S]) + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g));
         const uint32_t t2 = (rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22)) + ((a & b) | (c & (a | b)));
         h = g;
         g = f;

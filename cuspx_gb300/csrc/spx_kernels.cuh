@@ -183,46 +183,59 @@ __global__ void k_sign_msg(SetParams P, SignArgs A) {
     A.work[i] = work_from_digest<HF>(P, dg, sk + 2 * N);
 }
 
-// Two warps per signature for long messages (SHA-256 sets): the same
-// PRF_msg and H_msg as k_sign_msg, each message pass split into a
-// schedule-building warp and a rounds warp (Sha2::stream_msg_pair).  Blocks
-// whose message is shorter than long_msg return at once.
+// Long messages (SHA-256 sets): a 64-thread block takes 32 consecutive items
+// and hashes those of at least long_msg bytes with the same PRF_msg and H_msg
+// as k_sign_msg, each message pass split between lane l of the schedule warp
+// and lane l of the rounds warp (Sha2::stream_msg_pair); shorter items are
+// k_sign_msg's.  Per message the issue work is that of one thread, spread
+// over two warps, so latency drops without costing throughput.
 template <class HF>
 __global__ void __launch_bounds__(64) k_sign_msg_pair(SetParams P, SignArgs A) {
     constexpr int W = HF::W, N = 4 * W;
-    __shared__ uint32_t kw[128];
-    __shared__ uint32_t xr[8];
-    const uint32_t i = blockIdx.x;
-    if (i >= A.count || A.msg.len[i] < A.long_msg) return;   // uniform over the block
-    const int role = threadIdx.x == 0 ? 0 : (threadIdx.x == 32 ? 1 : 2);
-    const uint8_t *sk = A.sk.row(i);
-    uint32_t skprf[W], opt[W], pre[3 * W];
-    HF::load(skprf, sk + N);
-    if (A.optrand) {
-        HF::load(opt, A.optrand + (uint64_t)i * N);
-    } else {
+    __shared__ uint32_t kw[2 * 64 * 32];
+    __shared__ uint32_t xr[8 * 32];
+    const uint32_t l = threadIdx.x & 31;
+    const uint32_t i = blockIdx.x * 32 + l;
+    const uint64_t mlen = i < A.count ? A.msg.len[i] : 0;
+    const bool mine = i < A.count && mlen >= A.long_msg;
+    // both warps see the same 32 items, so these are uniform over the block
+    if (!__any_sync(0xffffffffu, mine)) return;
+    const int role = !mine ? 2 : (threadIdx.x < 32 ? 0 : 1);
+    uint64_t most = mine ? HF::template msg_blocks<3 * W>(mlen) : 0;
 #pragma unroll
-        for (int j = 0; j < W; j++) opt[j] = 0xadadadadu;
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t x = __shfl_xor_sync(0xffffffffu, most, o);
+        most = x > most ? x : most;
     }
-    const uint8_t *m = A.msg.base + A.msg.off[i];
-    const uint64_t mlen = A.msg.len[i];
-    uint32_t st[8];
+    const uint8_t *sk = mine ? A.sk.row(i) : nullptr;
+    const uint8_t *m = mine ? A.msg.base + A.msg.off[i] : nullptr;
+    uint32_t skprf[W], opt[W], pre[3 * W], st[8];
+#pragma unroll
+    for (int j = 0; j < W; j++) skprf[j] = opt[j] = 0xadadadadu;
+#pragma unroll
+    for (int j = 0; j < 3 * W; j++) pre[j] = 0;
+    if (mine) {
+        HF::load(skprf, sk + N);
+        if (A.optrand) HF::load(opt, A.optrand + (uint64_t)i * N);
+    }
     if (role == 1) HF::hmac_start(st, skprf);
-    HF::template stream_msg_pair<W>(st, 1, opt, m, mlen, kw, role);
+    HF::template stream_msg_pair<W>(st, 1, opt, m, mlen, kw, role, most);
     if (role == 1) {
         uint32_t R[W];
         HF::hmac_finish(R, st, skprf);
         HF::store(A.sig + (uint64_t)i * P.sig_bytes, R);
 #pragma unroll
-        for (int j = 0; j < W; j++) xr[j] = R[j];
+        for (int j = 0; j < W; j++) xr[j * 32 + l] = R[j];
     }
     __syncthreads();
+    if (mine) {
 #pragma unroll
-    for (int j = 0; j < W; j++) pre[j] = xr[j];
-    HF::load(pre + W, sk + 2 * N);
-    HF::load(pre + 2 * W, sk + 3 * N);
+        for (int j = 0; j < W; j++) pre[j] = xr[j * 32 + l];
+        HF::load(pre + W, sk + 2 * N);
+        HF::load(pre + 2 * W, sk + 3 * N);
+    }
     if (role == 1) sha256_iv(st);
-    HF::template stream_msg_pair<3 * W>(st, 0, pre, m, mlen, kw, role);
+    HF::template stream_msg_pair<3 * W>(st, 0, pre, m, mlen, kw, role, most);
     if (role == 1) {
         uint8_t dg[64];
         HF::mgf1_digest(dg, P.dgst_bytes, st);
@@ -755,23 +768,37 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A) {
     A.work[i] = work_from_digest<HF>(P, dg, pkb);
 }
 
-// H_msg of long messages over two warps (SHA-256 sets), as k_sign_msg_pair
+// H_msg of long messages over two warps (SHA-256 sets), 32 items per
+// block as in k_sign_msg_pair
 template <class HF>
 __global__ void __launch_bounds__(64) k_verify_msg_pair(SetParams P, VerifyArgs A) {
     constexpr int W = HF::W, N = 4 * W;
-    __shared__ uint32_t kw[128];
-    const uint32_t i = blockIdx.x;
-    if (i >= A.count || A.msg.len[i] < A.long_msg) return;   // uniform over the block
-    if (A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes) return;   // k_verify_msg rejected it
-    const int role = threadIdx.x == 0 ? 0 : (threadIdx.x == 32 ? 1 : 2);
-    const uint8_t *pkb = A.pk.row(i);
-    uint32_t pre[3 * W];
-    HF::load(pre, A.sig + (uint64_t)i * A.sig_stride);
-    HF::load(pre + W, pkb);
-    HF::load(pre + 2 * W, pkb + N);
-    uint32_t st[8];
+    __shared__ uint32_t kw[2 * 64 * 32];
+    const uint32_t l = threadIdx.x & 31;
+    const uint32_t i = blockIdx.x * 32 + l;
+    const uint64_t mlen = i < A.count ? A.msg.len[i] : 0;
+    // wrong-length signatures were rejected by k_verify_msg without hashing
+    const bool mine = i < A.count && mlen >= A.long_msg && !(A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes);
+    if (!__any_sync(0xffffffffu, mine)) return;   // uniform over the block
+    const int role = !mine ? 2 : (threadIdx.x < 32 ? 0 : 1);
+    uint64_t most = mine ? HF::template msg_blocks<3 * W>(mlen) : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t x = __shfl_xor_sync(0xffffffffu, most, o);
+        most = x > most ? x : most;
+    }
+    const uint8_t *pkb = mine ? A.pk.row(i) : nullptr;
+    uint32_t pre[3 * W], st[8];
+#pragma unroll
+    for (int j = 0; j < 3 * W; j++) pre[j] = 0;
+    if (mine) {
+        HF::load(pre, A.sig + (uint64_t)i * A.sig_stride);
+        HF::load(pre + W, pkb);
+        HF::load(pre + 2 * W, pkb + N);
+    }
     if (role == 1) sha256_iv(st);
-    HF::template stream_msg_pair<3 * W>(st, 0, pre, A.msg.base + A.msg.off[i], A.msg.len[i], kw, role);
+    HF::template stream_msg_pair<3 * W>(st, 0, pre, mine ? A.msg.base + A.msg.off[i] : nullptr, mlen, kw, role,
+                                        most);
     if (role == 1) {
         uint8_t dg[64];
         HF::mgf1_digest(dg, P.dgst_bytes, st);

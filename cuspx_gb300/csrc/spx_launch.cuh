@@ -177,7 +177,7 @@ struct Family {
         CUSPX_MARK(pt, "k_sign_msg", s);
         if constexpr (!HF::kShake) {
             if (A.long_msg) {
-                k_sign_msg_pair<HF><<<A.count, 64, 0, s>>>(P, A);
+                k_sign_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A);
                 CUSPX_MARK(pt, "k_sign_msg_pair", s);
             }
         }
@@ -212,7 +212,7 @@ struct Family {
         CUSPX_MARK(pt, "k_verify_msg", s);
         if constexpr (!HF::kShake) {
             if (A.long_msg) {
-                k_verify_msg_pair<HF><<<A.count, 64, 0, s>>>(P, A);
+                k_verify_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A);
                 CUSPX_MARK(pt, "k_verify_msg_pair", s);
             }
         }

@@ -433,33 +433,41 @@ struct Sha2 {
         }
     }
 
-    // The same absorption split over two warps of a 64-thread block, for long
-    // messages: one thread hashing alone is bound by its own instruction
-    // issue, about 1.3k ALU instructions per block.  Thread 0 (role 0) builds
-    // each block and its schedule with the round constants added into kw (a
-    // shared 2 x 64-word double buffer); thread 32 (role 1) runs the 64 rounds
-    // from kw a block behind; one __syncthreads per block hands a buffer over.
-    // Every thread of the block calls this with the same arguments (other
-    // threads pass role 2 and only take part in the barriers); the result is
-    // in role 1's st.
+    // The same absorption split over the two warps of a 64-thread block that
+    // hashes 32 messages, for long messages: a thread hashing alone is bound
+    // by its own instruction issue, about 1.3k ALU instructions per block.
+    // For message l, lane l of warp 0 (role 0) builds each block and its
+    // schedule with the round constants added into kw, and lane l of warp 1
+    // (role 1) runs the 64 rounds from kw a block behind; one __syncthreads
+    // per block hands a buffer over.  kw is a shared 2 x 64 x 32-word double
+    // buffer with the 32 messages interleaved (kw[(buf * 64 + t) * 32 + l]).
+    // Every thread of the block calls this; max_blocks (the same for the
+    // whole block) bounds the loop, and threads whose message has fewer
+    // blocks, or role 2, only take part in the barriers.  The result is in
+    // role 1's st.
     template <int P>
     SPX_DEV static void stream_msg_pair(uint32_t st[8], uint32_t pre_blocks, const uint32_t pre[P],
-                                        const uint8_t *m, uint64_t mlen, uint32_t *kw, int role) {
+                                        const uint8_t *m, uint64_t mlen, uint32_t *kw, int role,
+                                        uint64_t max_blocks) {
         const uint64_t dbytes = 4 * (uint64_t)P + mlen;
         const uint64_t nblocks = (dbytes + 9 + 63) / 64;
         const uint64_t bits = (64 * (uint64_t)pre_blocks + dbytes) * 8;
+        uint32_t *mine = kw + (threadIdx.x & 31);
         uint32_t nxt[16];
         bool have = false;
-        for (uint64_t b = 0; b <= nblocks; b++) {
+        for (uint64_t b = 0; b <= max_blocks; b++) {
             if (role == 0 && b < nblocks) {
                 uint32_t w[16];
                 next_block<P>(w, b, nblocks, bits, pre, m, mlen, nxt, have);
-                sha256_schedule_kw(kw + 64 * (b & 1), w);
+                sha256_schedule_kw<32>(mine + 64 * 32 * (b & 1), w);
             }
-            if (role == 1 && b >= 1) sha256_compress_kw(st, kw + 64 * ((b - 1) & 1));
+            if (role == 1 && b >= 1 && b <= nblocks) sha256_compress_kw<32>(st, mine + 64 * 32 * ((b - 1) & 1));
             __syncthreads();
         }
     }
+    // blocks of prefix (P words) || m with SHA-256 padding
+    template <int P>
+    SPX_DEV static uint64_t msg_blocks(uint64_t mlen) { return (4 * (uint64_t)P + mlen + 9 + 63) / 64; }
 
     // PRF_msg = HMAC-SHA256(SK_PRF, optrand || m), truncated (hash_sha256.cu:99-145):
     // the inner hash starts from the key block xor ipad, the outer one hashes

@@ -513,8 +513,7 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.status = b->status;
         A.ends = b->ends;
         A.ends_cap = b->ends_cap;
-        A.long_msg = b->long_msgs ? kPairMsgBytes : 0;
-        ops.sign(P, A, tu, b->s, pt);
+        ops.sign(P, A, tu, b->s, pt, b->long_msgs ? kPairMsgBytes : 0);
     } else if (b->op == CUSPX_OP_VERIFY) {
         VerifyArgs A;
         A.count = cnt;
@@ -530,8 +529,7 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.wpk = b->wpk;
         A.cur_root = b->cur_root;
         A.ctr = b->ctr;
-        A.long_msg = b->long_msgs ? kPairMsgBytes : 0;
-        ops.verify(P, A, tu, b->s, pt);
+        ops.verify(P, A, tu, b->s, pt, b->long_msgs ? kPairMsgBytes : 0);
     } else {
         KeygenArgs K{cnt, b->keys, b->out, b->leaves, b->roots, b->ends, b->ends_cap};
         ops.keygen(P, K, tu, b->s, pt);

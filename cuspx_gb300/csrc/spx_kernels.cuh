@@ -82,8 +82,6 @@ struct SignArgs {
     int32_t *status;           // count
     uint8_t *ends = nullptr;   // chain-parallel scratch: ends_cap x d x 2^hp x len x n, or null
     uint32_t ends_cap = 0;
-    uint64_t long_msg = 0;     // messages of at least this many bytes are hashed by
-                               // k_sign_msg_pair instead of k_sign_msg (0: none)
 };
 
 // tree/leaf indices of hypertree layer L (sign.cu:1987-1988)
@@ -156,8 +154,12 @@ SPX_DEV SignWork work_from_digest(const SetParams &P, const uint8_t *dg, const u
 // ===========================================================================
 // message phase: thread per signature
 // ===========================================================================
+// Messages of at least long_msg bytes are left to k_sign_msg_pair (0: none).
+// The threshold is a kernel argument rather than a field of the argument
+// structs: a larger by-value VerifyArgs changed the register allocation of
+// the persistent verify kernel and made it ~20% slower.
 template <class HF>
-__global__ void k_sign_msg(SetParams P, SignArgs A) {
+__global__ void k_sign_msg(SetParams P, SignArgs A, uint64_t long_msg) {
     constexpr int W = HF::W, N = 4 * W;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.count) return;
@@ -174,7 +176,7 @@ __global__ void k_sign_msg(SetParams P, SignArgs A) {
     }
     const uint8_t *m = A.msg.base + A.msg.off[i];
     const uint64_t mlen = A.msg.len[i];
-    if (A.long_msg && mlen >= A.long_msg) return;   // k_sign_msg_pair hashes it
+    if (long_msg && mlen >= long_msg) return;   // k_sign_msg_pair hashes it
     HF::prf_msg(R, skprf, opt, m, mlen);
     uint8_t *sig = A.sig + (uint64_t)i * P.sig_bytes;
     HF::store(sig, R);
@@ -190,14 +192,14 @@ __global__ void k_sign_msg(SetParams P, SignArgs A) {
 // k_sign_msg's.  Per message the issue work is that of one thread, spread
 // over two warps, so latency drops without costing throughput.
 template <class HF>
-__global__ void __launch_bounds__(64) k_sign_msg_pair(SetParams P, SignArgs A) {
+__global__ void __launch_bounds__(64) k_sign_msg_pair(SetParams P, SignArgs A, uint64_t long_msg) {
     constexpr int W = HF::W, N = 4 * W;
     __shared__ uint32_t kw[2 * 64 * 32];
     __shared__ uint32_t xr[8 * 32];
     const uint32_t l = threadIdx.x & 31;
     const uint32_t i = blockIdx.x * 32 + l;
     const uint64_t mlen = i < A.count ? A.msg.len[i] : 0;
-    const bool mine = i < A.count && mlen >= A.long_msg;
+    const bool mine = i < A.count && mlen >= long_msg;
     // both warps see the same 32 items, so these are uniform over the block
     if (!__any_sync(0xffffffffu, mine)) return;
     const int role = !mine ? 2 : (threadIdx.x < 32 ? 0 : 1);
@@ -738,11 +740,10 @@ struct VerifyArgs {
     uint8_t *wpk;               // count x len x n: WOTS public key of the current layer
     uint8_t *cur_root;          // count x n: root of the layer below (FORS key for layer 0)
     uint32_t *ctr = nullptr;    // persistent verify: next item to take (zeroed per launch)
-    uint64_t long_msg = 0;      // as SignArgs::long_msg, for k_verify_msg_pair
 };
 
 template <class HF>
-__global__ void k_verify_msg(SetParams P, VerifyArgs A) {
+__global__ void k_verify_msg(SetParams P, VerifyArgs A, uint64_t long_msg) {
     constexpr int W = HF::W, N = 4 * W;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.count) return;
@@ -756,7 +757,7 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A) {
         A.work[i] = w;
         return;
     }
-    if (A.long_msg && A.msg.len[i] >= A.long_msg) return;   // k_verify_msg_pair hashes it
+    if (long_msg && A.msg.len[i] >= long_msg) return;   // k_verify_msg_pair hashes it
     const uint8_t *pkb = A.pk.row(i);
     const uint8_t *sig = A.sig + (uint64_t)i * A.sig_stride;
     uint32_t R[W], pk[2 * W];
@@ -771,14 +772,14 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A) {
 // H_msg of long messages over two warps (SHA-256 sets), 32 items per
 // block as in k_sign_msg_pair
 template <class HF>
-__global__ void __launch_bounds__(64) k_verify_msg_pair(SetParams P, VerifyArgs A) {
+__global__ void __launch_bounds__(64) k_verify_msg_pair(SetParams P, VerifyArgs A, uint64_t long_msg) {
     constexpr int W = HF::W, N = 4 * W;
     __shared__ uint32_t kw[2 * 64 * 32];
     const uint32_t l = threadIdx.x & 31;
     const uint32_t i = blockIdx.x * 32 + l;
     const uint64_t mlen = i < A.count ? A.msg.len[i] : 0;
     // wrong-length signatures were rejected by k_verify_msg without hashing
-    const bool mine = i < A.count && mlen >= A.long_msg && !(A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes);
+    const bool mine = i < A.count && mlen >= long_msg && !(A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes);
     if (!__any_sync(0xffffffffu, mine)) return;   // uniform over the block
     const int role = !mine ? 2 : (threadIdx.x < 32 ? 0 : 1);
     uint64_t most = mine ? HF::template msg_blocks<3 * W>(mlen) : 0;

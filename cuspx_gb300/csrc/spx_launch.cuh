@@ -58,8 +58,11 @@ struct PhaseTimer {
 
 struct FamilyOps {
     cudaError_t (*configure)();
-    void (*sign)(const SetParams &, const SignArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
-    void (*verify)(const SetParams &, const VerifyArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
+    // long_msg: messages of at least this many bytes are hashed two warps per
+    // 32 messages (SHA-256 sets; 0 or a SHAKE set: one thread each)
+    void (*sign)(const SetParams &, const SignArgs &, const Tuning &, cudaStream_t, PhaseTimer *, uint64_t long_msg);
+    void (*verify)(const SetParams &, const VerifyArgs &, const Tuning &, cudaStream_t, PhaseTimer *,
+                   uint64_t long_msg);
     void (*keygen)(const SetParams &, const KeygenArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
     int smem_words;    // per-thread T_l stream scratch
 };
@@ -169,15 +172,15 @@ struct Family {
         CUSPX_MARK(pt, "k_leaves", s);
     }
 
-    static void sign(const SetParams &P, const SignArgs &A0, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
-        if (A0.count == 0) return;
-        SignArgs A = A0;
-        if (HF::kShake) A.long_msg = 0;   // the two-warp message kernels are SHA-256 only
-        k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
+    static void sign(const SetParams &P, const SignArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
+                     uint64_t long_msg) {
+        if (A.count == 0) return;
+        if (HF::kShake) long_msg = 0;   // the two-warp message kernels are SHA-256 only
+        k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A, long_msg);
         CUSPX_MARK(pt, "k_sign_msg", s);
         if constexpr (!HF::kShake) {
-            if (A.long_msg) {
-                k_sign_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A);
+            if (long_msg) {
+                k_sign_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A, long_msg);
                 CUSPX_MARK(pt, "k_sign_msg_pair", s);
             }
         }
@@ -204,15 +207,15 @@ struct Family {
         CUSPX_MARK(pt, "k_sign_finish", s);
     }
 
-    static void verify(const SetParams &P, const VerifyArgs &A0, const Tuning &tu, cudaStream_t s, PhaseTimer *pt) {
-        if (A0.count == 0) return;
-        VerifyArgs A = A0;
-        if (HF::kShake) A.long_msg = 0;
-        k_verify_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A);
+    static void verify(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
+                       uint64_t long_msg) {
+        if (A.count == 0) return;
+        if (HF::kShake) long_msg = 0;
+        k_verify_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A, long_msg);
         CUSPX_MARK(pt, "k_verify_msg", s);
         if constexpr (!HF::kShake) {
-            if (A.long_msg) {
-                k_verify_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A);
+            if (long_msg) {
+                k_verify_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A, long_msg);
                 CUSPX_MARK(pt, "k_verify_msg_pair", s);
             }
         }

@@ -6,6 +6,8 @@
 // batch of thousands of signatures fills all 152 SMs:
 //
 //   k_sign_msg      thread / signature   PRF_msg, H_msg -> R, FORS digest, tree, leaf
+//   k_sign_msg_pair 2 warps / 32 sigs    the same for messages of >= 2 KiB (SHA-256):
+//                                        schedule warp + rounds warp per message
 //   k_fors_sign     2^g lanes / FORS tree leaves (PRF+F), per-lane subtree stack,
 //                                        g shuffle levels, auth path, root
 //   k_leaves        thread / XMSS leaf   WOTS+ key (len chains x 15 F) streamed into
@@ -14,6 +16,12 @@
 //                                        auth path, root (k_trees_lane: lane / tree)
 //   k_sign_finish   block / signature    FORS pk (T_k), WOTS signatures gathered
 //                                        from the recorded chains
+//
+// Verify: k_verify_msg (+ k_verify_msg_pair) -> k_verify_fors -> the
+// hypertree, either one persistent launch (k_verify_hyper, spx_verify.cuh;
+// the default for simple sets) or per-layer k_verify_chains + k_verify_root
+// (robust sets), or k_verify_ht (one thread per item over all layers).
+// Key generation reuses k_leaves / k_trees on the top layer.
 //
 // Reference structure followed (CPU form): crypto_sign_signature sign.cu:1924-1994,
 // fors_sign fors.cu:107-143, treehash utils.cu:189-241, wots_gen_leaf sign.cu:87-102,

@@ -448,6 +448,8 @@ def served_runs(c, eng, peak_ops, seconds=2.0):
     _, sks = eng.keypair_batch(sid, seeds)
     srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000)
     srv.add_keys(sid, sks)
+    for op in (c.OP_SIGN, c.OP_VERIFY):
+        srv.prepare(op, sid)   # launch slots exist before the first timed request
     pts = []
     # 300k and 400k req/s offered are past what the GPU can serve at this mix
     # (~430k req/s of pure compute): they show the served roofline fraction
@@ -470,6 +472,8 @@ def served_runs(c, eng, peak_ops, seconds=2.0):
         z2 = c.set_sizes(s2)
         _, sk2 = eng.keypair_batch(s2, [rng.bytes(z2["seed"]) for _ in range(per)])
         srv.add_keys(s2, sk2)
+        for op in (c.OP_SIGN, c.OP_VERIFY):
+            srv.prepare(op, s2)
     pts = []
     for rate in (5e3, 20e3, 50e3, 100e3, 200e3):
         r = srv.loadgen(rate, seconds, sids, per, verify_frac=0.7, min_len=16, max_len=1 << 20, corrupt_frac=0.0,

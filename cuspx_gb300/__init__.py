@@ -399,7 +399,8 @@ class LoadgenResult(ctypes.Structure):
                 for f, _ in self._fields_}
 
 
-SERVE_EXPORTS = ["cuspx_serve_create", "cuspx_serve_destroy", "cuspx_serve_add_keys", "cuspx_serve_add_pubkeys",
+SERVE_EXPORTS = ["cuspx_serve_create", "cuspx_serve_destroy", "cuspx_serve_add_keys", "cuspx_serve_prepare",
+                 "cuspx_serve_add_pubkeys",
                  "cuspx_serve_submit", "cuspx_serve_wait", "cuspx_serve_stats", "cuspx_serve_reset_stats",
                  "cuspx_serve_loadgen"]
 
@@ -412,6 +413,7 @@ def _bind_serve(L):
     L.cuspx_serve_destroy.argtypes = [vp]
     L.cuspx_serve_destroy.restype = None
     L.cuspx_serve_add_keys.argtypes = [vp, c.c_int, c.c_size_t, vp, c.POINTER(c.c_uint32)]
+    L.cuspx_serve_prepare.argtypes = [vp, c.c_int, c.c_int]
     L.cuspx_serve_add_pubkeys.argtypes = [vp, c.c_int, c.c_size_t, vp, c.POINTER(c.c_uint32)]
     L.cuspx_serve_submit.argtypes = [vp, c.c_int, c.c_int, c.c_uint32, vp, c.c_size_t, vp, c.c_size_t, c.c_uint,
                                      c.POINTER(c.c_uint64)]
@@ -452,6 +454,10 @@ class Server:
         self.eng._check(self.L.cuspx_serve_add_keys(self.h, sid, len(sks), _buf(b), ctypes.byref(first)),
                         "serve_add_keys")
         return list(range(first.value, first.value + len(sks)))
+
+    def prepare(self, op, sid):
+        """Create every launch slot of (op, set) now rather than on first use."""
+        self.eng._check(self.L.cuspx_serve_prepare(self.h, op, sid), "serve_prepare")
 
     def add_pubkeys(self, sid, pks):
         b = b"".join(bytes(x) for x in pks)

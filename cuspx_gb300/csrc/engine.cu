@@ -163,6 +163,7 @@ struct cuspx_batch {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     bool ran = false;
     bool profile = false;
+    bool direct = false;   // never capture graphs (serving: see batch_direct_launch)
     bool prof_pending = false;
     PhaseTimer pt;
     std::vector<ProfEntry> prof;
@@ -569,6 +570,14 @@ int cuspx_batch_run(cuspx_batch *b) {
         b->ran = true;
         return CUSPX_OK;
     }
+    if (b->direct) {
+        CK(cudaEventRecord(b->e0, b->s), ctx);
+        launch_seq(b, nullptr);
+        CK(cudaGetLastError(), ctx);
+        CK(cudaEventRecord(b->e1, b->s), ctx);
+        b->ran = true;
+        return CUSPX_OK;
+    }
     const Tuning &tu = ctx->tune[b->set];
     cuspx_batch::GraphKey key{b->count, b->use_keyrow, b->use_aux, b->use_siglen, b->long_msgs, b->bound_keys, tu};
     b->use_clock++;
@@ -662,6 +671,16 @@ void *cuspx_batch_stream(cuspx_batch *b) { return b ? (void *)b->s : nullptr; }
 }  // extern "C"
 
 namespace cuspx {
+// Library-internal: launch this batch's kernels directly, never as a
+// captured graph.  Serving sees a different item count on almost every
+// launch, so it would capture and instantiate graphs while other launches
+// run; instantiation can wait for work already on the GPU (tens of ms behind
+// a long-message kernel) and holds the driver meanwhile, stalling every
+// thread's CUDA calls.  A direct launch of the 4-8 kernels costs tens of us.
+void batch_direct_launch(cuspx_batch *b, bool on) {
+    if (b) b->direct = on;
+}
+
 // Library-internal: give an idle batch a stream of the given priority (lower
 // numbers run first); its captured graphs are dropped with the old stream.
 int batch_set_stream_priority(cuspx_batch *b, int priority) {

@@ -3,10 +3,13 @@
 // memory-budgeted admission, per-request latency, and an open-loop Poisson
 // load generator.
 //
-// Threads: callers submit and wait under one mutex; a single scheduler
-// thread owns every CUDA call on the serving batches (pack into pinned
-// staging, upload, graph launch, asynchronous download, completion by event
-// query), so batch objects are never shared between threads.
+// Threads: callers submit and wait under one mutex; two scheduler threads,
+// one per message-length class, own every CUDA call on the serving batches
+// of their groups (pack into pinned staging, upload, graph launch,
+// asynchronous download, completion by event query), so a batch object is
+// only ever touched by one thread.  Packing a long-message launch copies up
+// to 64 MiB into pinned staging; with one scheduler, short launches and
+// completions waited behind that host work.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,6 +33,7 @@
 namespace cuspx {
 SetParams make_params(const SetDesc &s);
 int batch_set_stream_priority(cuspx_batch *b, int priority);
+void batch_direct_launch(cuspx_batch *b, bool on);
 }
 using namespace cuspx;
 using Clock = std::chrono::steady_clock;
@@ -107,8 +111,8 @@ struct cuspx_server {
     cuspx_serve_config cfg{};
     int device = 0;
     std::mutex mu;
-    std::condition_variable cv_sched, cv_done;
-    std::thread th;
+    std::condition_variable cv_sched[2], cv_done;   // cv_sched[length class]
+    std::thread th[2];
     bool stop = false;
     std::vector<KeyTable> keys;
     std::vector<Group> groups;   // index ((op - 1) * kNumSets + set) * 2 + long_class
@@ -167,6 +171,7 @@ static bool size_slot(cuspx_server *s, Group &g, Slot *sl) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     batch_set_stream_priority(sl->b, g.long_class ? lo : hi);
+    batch_direct_launch(sl->b, true);   // no graph instantiation while serving
     const KeyTable &kt = s->keys[g.set];
     cuspx_batch_bind_keys(sl->b, g.op == CUSPX_OP_SIGN ? kt.d_sk : kt.d_pk, kt.cap);
     auto host = [](void **p, size_t bytes) { return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };
@@ -259,7 +264,8 @@ static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
     sl->busy = false;
 }
 
-static void scheduler(cuspx_server *s) {
+// Scheduler of the groups of one length class (lc).
+static void scheduler(cuspx_server *s, int lc) {
     cudaSetDevice(s->device);
     const auto window = std::chrono::microseconds(s->cfg.window_us);
     const auto drain_deadline_len = std::chrono::seconds(60);
@@ -268,7 +274,10 @@ static void scheduler(cuspx_server *s) {
     while (true) {
         // ---- retire finished launches ----
         bool any_busy = false;
+        size_t class_pending = 0;
         for (Group &g : s->groups) {
+            if (g.long_class != lc) continue;
+            class_pending += g.pending.size();
             for (Slot *sl : g.slots) {
                 if (!sl->busy) continue;
                 cudaError_t e = cudaEventQuery(sl->ev);
@@ -282,12 +291,13 @@ static void scheduler(cuspx_server *s) {
         }
         if (s->stop) {
             if (drain_deadline == Clock::time_point{}) drain_deadline = Clock::now() + drain_deadline_len;
-            if ((!any_busy && s->pending_total == 0) || Clock::now() > drain_deadline) break;
+            if ((!any_busy && class_pending == 0) || Clock::now() > drain_deadline) break;
         }
         // ---- admit new launches ----
         const auto now = Clock::now();
         Clock::time_point next_wake = now + std::chrono::microseconds(50);
         for (Group &g : s->groups) {
+            if (g.long_class != lc) continue;
             while (!g.pending.empty()) {
                 int inflight = 0;
                 Slot *free_sl = nullptr;
@@ -342,7 +352,7 @@ static void scheduler(cuspx_server *s) {
                 }
             }
         }
-        s->cv_sched.wait_until(lk, next_wake);
+        s->cv_sched[lc].wait_until(lk, next_wake);
     }
 }
 
@@ -372,7 +382,8 @@ int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_serv
                 g.P = make_params(kSets[set]);
                 g.per_item = item_bytes(op, g.P);
             }
-    s->th = std::thread(scheduler, s);
+    s->th[0] = std::thread(scheduler, s, 0);
+    s->th[1] = std::thread(scheduler, s, 1);
     *out = s;
     return CUSPX_OK;
 }
@@ -383,8 +394,9 @@ void cuspx_serve_destroy(cuspx_server *s) {
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
     }
-    s->cv_sched.notify_all();
-    if (s->th.joinable()) s->th.join();
+    for (int lc = 0; lc < 2; lc++) s->cv_sched[lc].notify_all();
+    for (int lc = 0; lc < 2; lc++)
+        if (s->th[lc].joinable()) s->th[lc].join();
     for (Group &g : s->groups) {
         for (Slot *sl : g.slots) {
             if (sl->busy && sl->b) cuspx_batch_sync(sl->b);
@@ -401,18 +413,26 @@ void cuspx_serve_destroy(cuspx_server *s) {
     delete s;
 }
 
+// The set's resident key table, allocated once at max_keys rows (so the
+// device address the slots are bound to never changes); lock held.
+static int ensure_table(cuspx_server *s, int set) {
+    KeyTable &kt = s->keys[set];
+    if (kt.d_sk) return CUSPX_OK;
+    const size_t n = kSets[set].n;
+    kt.cap = s->cfg.max_keys;
+    if (cudaMalloc(&kt.d_sk, kt.cap * 4 * n) != cudaSuccess || cudaMalloc(&kt.d_pk, kt.cap * 2 * n) != cudaSuccess)
+        return CUSPX_ENOMEM;
+    cudaMemset(kt.d_sk, 0, kt.cap * 4 * n);
+    cudaMemset(kt.d_pk, 0, kt.cap * 2 * n);
+    return CUSPX_OK;
+}
+
 static int add_rows(cuspx_server *s, int set, size_t count, const uint8_t *rows, bool secret, uint32_t *first) {
     if (!s || set < 0 || set >= kNumSets || (count && !rows)) return CUSPX_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
     KeyTable &kt = s->keys[set];
     const size_t n = kSets[set].n;
-    if (!kt.d_sk) {
-        kt.cap = s->cfg.max_keys;
-        if (cudaMalloc(&kt.d_sk, kt.cap * 4 * n) != cudaSuccess || cudaMalloc(&kt.d_pk, kt.cap * 2 * n) != cudaSuccess)
-            return CUSPX_ENOMEM;
-        cudaMemset(kt.d_sk, 0, kt.cap * 4 * n);
-        cudaMemset(kt.d_pk, 0, kt.cap * 2 * n);
-    }
+    if (int rc = ensure_table(s, set)) return rc;
     if (kt.n + count > kt.cap) return CUSPX_ENOMEM;
     for (size_t i = 0; i < count; i++) {
         const uint8_t *r = rows + i * (secret ? 4 * n : 2 * n);
@@ -426,6 +446,30 @@ static int add_rows(cuspx_server *s, int set, size_t count, const uint8_t *rows,
     }
     if (first) *first = (uint32_t)kt.n;
     kt.n += count;
+    return CUSPX_OK;
+}
+
+// Create every launch slot of (op, set) -- both length classes, max_inflight
+// each -- now instead of on first use: a slot's device batch and pinned
+// staging (64 MiB for long messages) take milliseconds to allocate, and
+// device allocation can wait for work already on the GPU, so creating them
+// while requests flow puts that time on the requests' latency.
+int cuspx_serve_prepare(cuspx_server *s, int op, int set) {
+    if (!s || (op != CUSPX_OP_SIGN && op != CUSPX_OP_VERIFY) || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    if (cudaSetDevice(s->device) != cudaSuccess) return CUSPX_ECUDA;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (int rc = ensure_table(s, set)) return rc;
+    for (int lc = 0; lc < 2; lc++) {
+        Group &g = s->groups[((op - 1) * kNumSets + set) * 2 + lc];
+        while ((int)g.slots.size() < s->cfg.max_inflight) {
+            Slot *sl = new Slot();
+            if (!size_slot(s, g, sl)) {
+                free_slot(sl);
+                return CUSPX_ENOMEM;
+            }
+            g.slots.push_back(sl);
+        }
+    }
     return CUSPX_OK;
 }
 
@@ -485,7 +529,7 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     if (ticket) *ticket = r->ticket;
     const bool kick = g.pending.size() == 1 || g.pending.size() >= (size_t)s->cfg.max_batch;
     lk.unlock();
-    if (kick) s->cv_sched.notify_one();
+    if (kick) s->cv_sched[g.long_class].notify_one();
     return CUSPX_OK;
 }
 

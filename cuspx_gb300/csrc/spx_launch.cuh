@@ -103,6 +103,21 @@ struct Family {
         if constexpr (kPersistVerify)
             if ((e = cudaFuncSetAttribute(k_verify_hyper<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big)))
                 return e;
+        // Load every other kernel of the family now: with lazy module loading
+        // a kernel's first launch loads it, and in a server that first launch
+        // is a request's (one took ~50 ms of host time and held back every
+        // queued request of its class).
+        cudaFuncAttributes fa;
+        const void *rest[] = {(const void *)k_sign_msg<HF>, (const void *)k_leaf_chains<HF>,
+                              (const void *)k_trees_lane<HF>, (const void *)k_sign_finish<HF>,
+                              (const void *)k_verify_msg<HF>, (const void *)k_verify_fors<HF>,
+                              (const void *)k_verify_chains<HF>, (const void *)k_keygen_finish<N>};
+        for (const void *f : rest)
+            if ((e = cudaFuncGetAttributes(&fa, f))) return e;
+        if constexpr (!HF::kShake) {
+            if ((e = cudaFuncGetAttributes(&fa, (const void *)k_sign_msg_pair<HF>))) return e;
+            if ((e = cudaFuncGetAttributes(&fa, (const void *)k_verify_msg_pair<HF>))) return e;
+        }
         return cudaSuccess;
     }
 

@@ -5,8 +5,9 @@
  * that allocate, launch and free per batch (sign.cu:5920-5963).  Here
  * requests are admitted as they arrive and continuously batched:
  *   - keys live on the device in a per-set resident table (sk and pk rows);
- *   - a scheduler thread groups pending requests per (operation, set) and
- *     launches a batch when the batch is full, the oldest request has waited
+ *   - scheduler threads (one for messages up to 16 KiB, one for longer
+ *     ones) group pending requests per (operation, set, length class) and
+ *     launch a batch when the batch is full, the oldest request has waited
  *     `window_us`, or no launch of that group is in flight;
  *   - up to `max_inflight` launches per group run at once on their own
  *     streams, so requests arriving while others are on the GPU are admitted
@@ -67,6 +68,12 @@ void cuspx_serve_destroy(cuspx_server *s);
 /* resident keys: count secret keys (4n bytes each) of `set`; ids are
  * consecutive from *first_id.  The public key of each is its sk[2n..4n). */
 int cuspx_serve_add_keys(cuspx_server *s, int set, size_t count, const uint8_t *sks, uint32_t *first_id);
+/* Create every launch slot of (op, set) now -- the device batch and pinned
+ * staging of up to max_inflight launches for each message-length class --
+ * instead of when the first requests need them, so that no allocation falls
+ * on the serving path (device allocation can wait for the GPU).  Optional;
+ * no counterpart in the reference, whose GPU faces allocate per call. */
+int cuspx_serve_prepare(cuspx_server *s, int op, int set);
 /* public-only keys for verification (2n bytes each); signing with them fails */
 int cuspx_serve_add_pubkeys(cuspx_server *s, int set, size_t count, const uint8_t *pks, uint32_t *first_id);
 /* op: CUSPX_OP_SIGN (sig ignored) or CUSPX_OP_VERIFY (sig/siglen checked) */

@@ -130,3 +130,33 @@ def test_loadgen_short_run(engine):
         assert r["completed"] + r["refused"] == r["offered"] and r["offered"] > 500
     finally:
         srv.close()
+
+
+def test_prepared_slots_serve_the_same_bytes(engine):
+    """cuspx_serve_prepare creates a set's launch slots (and its key table)
+    before any key or request; keys added afterwards are served through the
+    prepared slots, short and long messages alike, with the oracle's bytes."""
+    import cuspx_gb300 as c
+    import spx_oracle
+    name = "sha256-128f-simple"
+    sid = c.set_id(name)
+    keys = _setup(engine, [name], 2, seed=21)
+    pks, sks, z = keys[sid]
+    o = spx_oracle.Oracle(name)
+    rng = random.Random(23)
+    srv = c.Server(engine, max_batch=32, max_inflight=2, window_us=200)
+    try:
+        for op in (c.OP_SIGN, c.OP_VERIFY):
+            srv.prepare(op, sid)
+            srv.prepare(op, sid)   # a second call finds every slot there
+        ids = srv.add_keys(sid, sks)
+        msgs = [bytes(rng.randrange(256) for _ in range(L)) for L in (10, 3000, 20000)]
+        tickets = [srv.submit(c.OP_SIGN, sid, ids[1], m) for m in msgs]
+        for m, t in zip(msgs, tickets):
+            sig, st, _ = srv.wait(t, 60_000_000, z["sig"])
+            assert st == 0 and sig == o.sign(m, sks[1])
+            tv = srv.submit(c.OP_VERIFY, sid, ids[1], m, sig)
+            _, vst, _ = srv.wait(tv, 60_000_000, 0)
+            assert vst == 0
+    finally:
+        srv.close()

@@ -238,7 +238,11 @@ int cuspx_create(int device, cuspx_ctx **out) {
         t.tree_mode = sd.h / sd.d <= 4 ? 1 : 0;
         t.leaf_block = (sd.hash == 0 && !sd.robust) ? 256 : 128;
         t.chains_per_warp = sd.hash == 1 ? 256 : 128;
-        t.verify_mode = sd.robust ? 0 : 2;
+        t.verify_mode = (sd.robust && sd.hash == 0) ? 0 : 2;
+        // a robust SHAKE item is two units per F and H: fewer items per warp
+        // keep enough warps busy (16384 SHAKE-256f-robust: 2 slots 93.9 ms,
+        // 4 slots 98.9 ms)
+        if (sd.robust && sd.hash == 1) t.verify_slots = 2;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;

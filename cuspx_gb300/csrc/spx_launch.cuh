@@ -121,8 +121,9 @@ struct Family {
         return cudaSuccess;
     }
 
-    // the persistent verify kernel covers the simple sets of both hashes
-    static constexpr bool kPersistVerify = !HF::kRobust;
+    // the persistent verify kernel covers the simple sets of both hashes and
+    // the robust SHAKE-256 sets
+    static constexpr bool kPersistVerify = !HF::kRobust || HF::kShake;
 
     // one launch over the batch's whole hypertree: as many blocks as are
     // resident at once (or fewer for small batches); warps take items from

@@ -108,6 +108,9 @@ struct VerifySha2 : VerifySlot<4 * HF::W, 22, 64> {
     static constexpr int stream_blocks(int m) { return (22 + m * N + 9 + 63) / 64; }
     static constexpr int kStreamWords = stream_blocks(LEN) * 16;
     static constexpr int kHBlocks = (22 + 2 * N + 9 + 63) / 64;   // H = SHA256(mid; ADRS_c || l || r)
+    // units per F step and per H; whether T absorbs a mask stream
+    static constexpr int kFUnits = 1, kHUnits = kHBlocks;
+    static constexpr bool kTMask = false;
     static __host__ __device__ int slot_words(int hp) { return B::S_HDR + kStreamWords + hp * W; }
 
     struct Unit {
@@ -173,7 +176,7 @@ struct VerifySha2 : VerifySlot<4 * HF::W, 22, 64> {
         for (int i = 0; i < 8; i++) r.kmid[i] = r.tst[i] = S[B::S_KEY + i];
     }
 
-    SPX_DEV static void build_chain(Unit &u, const LaneRegs &r, const uint32_t *S, int c, int s,
+    SPX_DEV static void build_chain(Unit &u, const LaneRegs &r, const uint32_t *S, int c, int s, int,
                                     const uint32_t v[W]) {
 #pragma unroll
         for (int i = 0; i < 8; i++) u.st[i] = r.kmid[i];
@@ -285,6 +288,8 @@ struct VerifyShake : VerifySlot<4 * HF::W, 4 * HF::W + 32, 136> {
     static constexpr int stream_blocks(int m) { return (8 * kPreLanes + m * N) / 136 + 1; }
     static constexpr int kStreamWords = stream_blocks(LEN) * 34;
     static constexpr int kHBlocks = 1;
+    static constexpr int kFUnits = 1, kHUnits = 1;
+    static constexpr bool kTMask = false;
     static constexpr int kTStateWords = 50;
     static __host__ __device__ int slot_words(int hp) { return B::S_HDR + kStreamWords + hp * W + kTStateWords; }
 
@@ -343,7 +348,7 @@ struct VerifyShake : VerifySlot<4 * HF::W, 4 * HF::W + 32, 136> {
         u.A[NL + 2] = lane_of(bswap32(aw[4]), bswap32(aw[5]));
         u.A[NL + 3] = 0;
     }
-    SPX_DEV static void build_chain(Unit &u, const LaneRegs &, const uint32_t *S, int c, int s,
+    SPX_DEV static void build_chain(Unit &u, const LaneRegs &, const uint32_t *S, int c, int s, int,
                                     const uint32_t v[W]) {
 #pragma unroll
         for (int i = 0; i < 25; i++) u.A[i] = 0;
@@ -406,8 +411,160 @@ struct VerifyShake : VerifySlot<4 * HF::W, 4 * HF::W + 32, 136> {
     SPX_DEV static void after_h_first(const Unit &, LaneRegs &) {}
 };
 
+// ---------------------------------------------------------------------------
+// SHAKE-256 robust (SPHINCS+ round-3 robust tweakable hash; the reference has
+// no robust thash): every F and H input is xored with a mask drawn from
+// SHAKE256(PUB_SEED || ADRS), and T_l absorbs its values xored with the
+// squeezed stream of SHAKE256(PUB_SEED || ADRS_T).  A chain step or an H is
+// two units (the mask permutation, then the hash); the T lane is claimed as
+// soon as its layer starts and squeezes the mask stream (one permutation per
+// 17 lanes) into the slot while the chains run, then absorbs each T block
+// once its chains and its mask lanes are there.
+// ---------------------------------------------------------------------------
 template <class HF>
-using VerifyPolicy = typename std::conditional<HF::kShake != 0, VerifyShake<HF>, VerifySha2<HF>>::type;
+struct VerifyShakeRobust : VerifyShake<HF> {
+    using S0 = VerifyShake<HF>;
+    using B = typename S0::B;
+    using Unit = typename S0::Unit;
+    static constexpr int W = S0::W, N = S0::N, NL = S0::NL, LEN = S0::LEN, kPreLanes = S0::kPreLanes;
+    static constexpr int kStreamWords = S0::kStreamWords;
+    static constexpr int kFUnits = 2, kHUnits = 2;
+    static constexpr bool kTMask = true;
+    enum : int { S_MB = 14 };   // header: mask blocks squeezed so far
+    static constexpr int mask_blocks(int m) { return (m * NL + 16) / 17; }
+    static constexpr int kMaskLanes = 17 * ((LEN * NL + 16) / 17);
+    static __host__ __device__ int slot_words(int hp) { return S0::slot_words(hp) + 50 + 2 * kMaskLanes; }
+
+    struct LaneRegs {
+        uint64_t mk[2 * NL];   // the current F or H mask
+    };
+
+    SPX_DEV static uint64_t *msponge(uint32_t *S, int hp) { return S0::tstate(S, hp) + 25; }
+    SPX_DEV static uint64_t *mlanes(uint32_t *S, int hp) { return S0::tstate(S, hp) + 50; }
+
+    SPX_DEV static void claim_chain(LaneRegs &, const uint32_t *) {}
+    SPX_DEV static void claim_t(LaneRegs &, uint32_t *S, int hp) {
+        uint64_t *T = S0::tstate(S, hp);
+#pragma unroll
+        for (int i = 0; i < 25; i++) T[i] = 0;
+        S[S_MB] = 0;
+    }
+
+    // mask unit: SHAKE256(PUB_SEED || ADRS) with nothing after the ADRS
+    SPX_DEV static void mask_unit(Unit &u, const uint32_t *S, const uint32_t aw[6]) {
+#pragma unroll
+        for (int i = 0; i < 25; i++) u.A[i] = 0;
+        S0::put_prefix(u, S, aw);
+        u.A[kPreLanes] = 0x1Full;
+        u.A[16] ^= 0x8000000000000000ull;
+    }
+    SPX_DEV static void build_chain(Unit &u, const LaneRegs &r, const uint32_t *S, int c, int s, int sub,
+                                    const uint32_t v[W]) {
+        const uint32_t aw[6] = {S[B::S_AW0], S[B::S_AW1], S[B::S_AW2], S[B::S_IDXL] << 16, (uint32_t)c << 16,
+                                (uint32_t)s << 16};
+        mask_unit(u, S, aw);
+        if (sub == 1) {
+            // the masked value replaces the mask unit's pad lane; the pad
+            // byte moves behind it (the 0x80 of lane 16 stays)
+#pragma unroll
+            for (int i = 0; i < NL; i++) u.A[kPreLanes + i] = lane_of(v[2 * i], v[2 * i + 1]) ^ r.mk[i];
+            u.A[kPreLanes + NL] = 0x1Full;
+        }
+    }
+    SPX_DEV static void after_f_first(const Unit &u, LaneRegs &r) {
+#pragma unroll
+        for (int i = 0; i < NL; i++) r.mk[i] = u.A[i];
+    }
+    SPX_DEV static void build_h(Unit &u, const LaneRegs &r, const uint32_t *S, int h, int sub, uint32_t idx,
+                                const uint32_t v[W], int) {
+        const uint32_t *auth = S + B::S_HDR + kStreamWords + h * W;
+        const bool right = idx & 1u;
+        Adrs a;
+        a.w[0] = S[B::S_AW0];
+        a.w[1] = S[B::S_AW1];
+        a.w[2] = (S[B::S_AW2] & 0xff000000u) | (ADDR_HASHTREE << 16);
+        a.w[3] = 0;
+        a.w[4] = 0;
+        a.w[5] = 0;
+        adrs_height(a, h + 1);
+        adrs_index(a, idx >> 1);
+        mask_unit(u, S, a.w);
+        if (sub == 1) {
+            // masked l || r replace the mask unit's pad lane; pad behind them
+#pragma unroll
+            for (int i = 0; i < NL; i++) {
+                const uint64_t sl = lane_of(auth[2 * i], auth[2 * i + 1]);
+                const uint64_t vl = lane_of(v[2 * i], v[2 * i + 1]);
+                u.A[kPreLanes + i] = (right ? sl : vl) ^ r.mk[i];
+                u.A[kPreLanes + NL + i] = (right ? vl : sl) ^ r.mk[NL + i];
+            }
+            u.A[kPreLanes + 2 * NL] ^= 0x1Full;
+        }
+    }
+    SPX_DEV static void after_h_first(const Unit &u, LaneRegs &r) {
+#pragma unroll
+        for (int i = 0; i < 2 * NL; i++) r.mk[i] = u.A[i];
+    }
+
+    // T lane's next unit for block j: 1 = a mask block (needed by block j, or
+    // ahead of the chains), 0 = block j, 2 = nothing ready
+    SPX_DEV static int t_action(const uint32_t *S, int j) {
+        const int m = (int)S[B::S_M];
+        const int mb = (int)S[S_MB];
+        const int hi = 17 * j + 16 - kPreLanes;   // last value lane of block j
+        const int last = hi < m * NL - 1 ? hi : m * NL - 1;
+        const int need = last < 0 ? 0 : last / 17 + 1;
+        if (mb < need) return 1;
+        if (B::done_prefix(S) > B::block_last_value(j, m)) return 0;
+        return mb < mask_blocks(m) ? 1 : 2;
+    }
+    SPX_DEV static void build_mask(Unit &u, uint32_t *S, int hp) {
+        if (S[S_MB] == 0) {
+            const uint64_t *L = S0::lanes(S + B::S_HDR);   // PUB_SEED || ADRS_T lanes of the stream
+#pragma unroll
+            for (int i = 0; i < 25; i++) u.A[i] = i < kPreLanes ? L[i < kPreLanes ? i : 0] : 0ull;
+            u.A[kPreLanes] = 0x1Full;
+            u.A[16] ^= 0x8000000000000000ull;
+        } else {
+            const uint64_t *M = msponge(S, hp);
+#pragma unroll
+            for (int i = 0; i < 25; i++) u.A[i] = M[i];
+        }
+    }
+    SPX_DEV static void after_mask(const Unit &u, uint32_t *S, int hp) {
+        uint64_t *M = msponge(S, hp);
+        uint64_t *ml = mlanes(S, hp) + 17 * S[S_MB];
+#pragma unroll
+        for (int i = 0; i < 25; i++) M[i] = u.A[i];
+#pragma unroll
+        for (int i = 0; i < 17; i++) ml[i] = u.A[i];
+        S[S_MB] = S[S_MB] + 1;
+    }
+    SPX_DEV static void after_t(const Unit &u, LaneRegs &, uint32_t *S, int hp) {
+        uint64_t *T = S0::tstate(S, hp);
+#pragma unroll
+        for (int i = 0; i < 25; i++) T[i] = u.A[i];
+    }
+    // T block j with its value lanes xored with the mask stream
+    SPX_DEV static void build_t(Unit &u, const LaneRegs &, uint32_t *S, int j, int hp) {
+        const uint64_t *T = S0::tstate(S, hp);
+        const uint64_t *b = S0::lanes(S + B::S_HDR) + 17 * j;
+        const uint64_t *ml = mlanes(S, hp);
+        const int nv = (int)S[B::S_M] * NL;
+#pragma unroll
+        for (int i = 0; i < 17; i++) {
+            const int q = 17 * j + i - kPreLanes;   // value lane index
+            u.A[i] = T[i] ^ b[i] ^ ((q >= 0 && q < nv) ? ml[q >= 0 && q < nv ? q : 0] : 0ull);
+        }
+#pragma unroll
+        for (int i = 17; i < 25; i++) u.A[i] = T[i];
+    }
+};
+
+template <class HF>
+using VerifyPolicy = typename std::conditional<
+    HF::kShake != 0, typename std::conditional<HF::kRobust, VerifyShakeRobust<HF>, VerifyShake<HF>>::type,
+    VerifySha2<HF>>::type;
 
 template <class HF>
 __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A, uint32_t *ctr, int G) {
@@ -425,7 +582,9 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
     // lane task state
     int kind = PV::K_NONE, tg = 0;   // task kind, slot
     int tc = 0;                      // chain index / T block / H step
-    int ts = 0;                      // chain step / H sub-block
+    int ts = 0;                      // chain step / H unit
+    int tsub = 0;                    // unit within a chain step (robust: mask, then F)
+    int tact = 0;                    // T lane's unit this iteration (robust: 0 block, 1 mask, 2 none)
     uint32_t tidx = 0;               // compute_root node index
     uint32_t v[W];                   // chain value / current node
 #pragma unroll
@@ -540,7 +699,9 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         for (int g = 0; g < G && need; g++) {
             uint32_t *S = slots + g * SW;
             if (S[PV::S_STATE] != PV::ACTIVE) continue;
-            if (S[PV::S_TCLAIM] == 0 && PV::done_prefix(S) > PV::block_last_value(0, (int)S[PV::S_M])) {
+            // (a masked T starts at once: its mask stream needs no chain)
+            if (S[PV::S_TCLAIM] == 0 &&
+                (PV::kTMask || PV::done_prefix(S) > PV::block_last_value(0, (int)S[PV::S_M]))) {
                 const int leader = __ffs(need) - 1;
                 if ((int)lane == leader) {
                     kind = PV::K_T;
@@ -569,6 +730,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                         tg = g;
                         tc = c;
                         ts = s0;
+                        tsub = 0;
                         PV::read_value(S + PV::S_HDR, c, v);
                         PV::claim_chain(lr, S);
                     }
@@ -587,11 +749,18 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         bool run = kind != PV::K_NONE;
         typename PV::Unit u;
         if (kind == PV::K_CHAIN) {
-            PV::build_chain(u, lr, S, tc, ts, v);
+            PV::build_chain(u, lr, S, tc, ts, tsub, v);
         } else if (kind == PV::K_T) {
-            // idle while the chains this block covers are still running
-            run = PV::done_prefix(S) > PV::block_last_value(tc, (int)S[PV::S_M]);
-            PV::build_t(u, lr, S, tc, P.hp);
+            if constexpr (PV::kTMask) {
+                tact = PV::t_action(S, tc);
+                run = tact != 2;
+                if (tact == 1) PV::build_mask(u, S, P.hp);
+                else PV::build_t(u, lr, S, tc, P.hp);
+            } else {
+                // idle while the chains this block covers are still running
+                run = PV::done_prefix(S) > PV::block_last_value(tc, (int)S[PV::S_M]);
+                PV::build_t(u, lr, S, tc, P.hp);
+            }
         } else if (kind == PV::K_ROOT) {
             PV::build_h(u, lr, S, tc, ts, tidx, v, P.hp);
         } else {
@@ -603,7 +772,21 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
 
         // ---- use the output ----
         bool slot_event = false;
-        if (run && kind == PV::K_CHAIN) {
+        bool step = true;   // the chain step's last unit ran
+        if constexpr (PV::kFUnits == 2) {
+            if (run && kind == PV::K_CHAIN) {
+                if (tsub == 0) PV::after_f_first(u, lr);
+                step = tsub == 1;
+                tsub ^= 1;
+            }
+        }
+        if constexpr (PV::kTMask) {
+            if (run && kind == PV::K_T && tact == 1) {
+                PV::after_mask(u, S, P.hp);
+                run = false;   // a mask unit does not advance the T stream
+            }
+        }
+        if (run && step && kind == PV::K_CHAIN) {
             PV::value_out(u, v);
             if (++ts >= 15) {
                 PV::write_value(S + PV::S_HDR, tc, v);
@@ -630,7 +813,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 }
             }
         } else if (run && kind == PV::K_ROOT) {
-            if (PV::kHBlocks == 2 && ts == 0) {
+            if (PV::kHUnits == 2 && ts == 0) {
                 PV::after_h_first(u, lr);
                 ts = 1;
             } else {

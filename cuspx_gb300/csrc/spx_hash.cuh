@@ -94,7 +94,12 @@ SPX_DEV uint32_t rotr(uint32_t x, int c) { return __funnelshift_r(x, x, c); }
 // shifts, LOP3 and IADD3 all issue there) while the FMA pipe idles.  An add
 // written as a * c_one + b with c_one an opaque constant-bank 1 must issue as
 // IMAD on the FMA pipe, so the 2-input adds (e = d + t1 each round, the last
-// add of each schedule word) move there.  CUSPX_FMA_ADDS=0 restores plain adds.
+// add of each schedule word, the schedule word into t1) move there.
+// Shifts and rotates stay on the ALU: as multiplies by 2^(32-k) from the
+// constant bank (x >> k = umulhi, rotr = x * m + umulhi) they measured
+// slower at every depth tried (k_leaves +0.2% for the sigma shifts alone,
+// +28% with five rotates per round moved), as IMAD.HI does not issue at
+// IMAD's rate.  CUSPX_FMA_ADDS=0 restores plain adds.
 #ifndef CUSPX_FMA_ADDS
 #define CUSPX_FMA_ADDS 1
 #endif
@@ -105,6 +110,20 @@ SPX_DEV uint32_t add_fma(uint32_t a, uint32_t b) {
 #else
     return a + b;
 #endif
+}
+
+// the four SHA-256 sigma functions (FIPS 180-4 4.4-4.7)
+SPX_DEV uint32_t sha_Sigma0(uint32_t a) {
+    return rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22);
+}
+SPX_DEV uint32_t sha_Sigma1(uint32_t e) {
+    return rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25);
+}
+SPX_DEV uint32_t sha_sigma0(uint32_t x) {
+    return rotr(x, 7) ^ rotr(x, 18) ^ (x >> 3);
+}
+SPX_DEV uint32_t sha_sigma1(uint32_t y) {
+    return rotr(y, 17) ^ rotr(y, 19) ^ (y >> 10);
 }
 
 SPX_DEV void sha256_iv(uint32_t s[8]) {
@@ -123,13 +142,12 @@ SPX_DEV void sha256_rounds(uint32_t st[8], uint32_t w[16]) {
         if (i < 16) {
             wi = w[i];
         } else {
-            uint32_t x = w[(i - 15) & 15], y = w[(i - 2) & 15];
-            uint32_t s0 = rotr(x, 7) ^ rotr(x, 18) ^ (x >> 3);
-            uint32_t s1 = rotr(y, 17) ^ rotr(y, 19) ^ (y >> 10);
-            wi = w[i & 15] = add_fma(w[i & 15], s0 + w[(i - 7) & 15] + s1);
+            wi = w[i & 15] = add_fma(w[i & 15], sha_sigma0(w[(i - 15) & 15]) + w[(i - 7) & 15] +
+                                                    sha_sigma1(w[(i - 2) & 15]));
         }
-        uint32_t t1 = h + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g)) + sha256_k(i) + wi;
-        uint32_t t2 = (rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22)) + ((a & b) | (c & (a | b)));
+        // h + K is ready a round early, so the schedule word joins it on the FMA pipe
+        uint32_t t1 = add_fma(h + sha256_k(i), wi) + sha_Sigma1(e) + ((e & f) ^ (~e & g));
+        uint32_t t2 = sha_Sigma0(a) + ((a & b) | (c & (a | b)));
         h = g;
         g = f;
         f = e;
@@ -150,10 +168,7 @@ SPX_DEV void sha256_schedule_kw(uint32_t *kw, uint32_t w[16]) {
 #pragma unroll
     for (int i = 0; i < 64; i++) {
         if (i >= 16) {
-            const uint32_t x = w[(i - 15) & 15], y = w[(i - 2) & 15];
-            const uint32_t s0 = rotr(x, 7) ^ rotr(x, 18) ^ (x >> 3);
-            const uint32_t s1 = rotr(y, 17) ^ rotr(y, 19) ^ (y >> 10);
-            w[i & 15] = w[i & 15] + s0 + w[(i - 7) & 15] + s1;
+            w[i & 15] = w[i & 15] + sha_sigma0(w[(i - 15) & 15]) + w[(i - 7) & 15] + sha_sigma1(w[(i - 2) & 15]);
         }
         kw[i * S] = add_fma(w[i & 15], sha256_k(i));
     }
@@ -166,8 +181,8 @@ SPX_DEV void sha256_compress_kw(uint32_t s[8], const uint32_t *kw) {
     uint32_t a = s[0], b = s[1], c = s[2], d = s[3], e = s[4], f = s[5], g = s[6], h = s[7];
 #pragma unroll
     for (int i = 0; i < 64; i++) {
-        const uint32_t t1 = add_fma(h, kw[i * S]) + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g));
-        const uint32_t t2 = (rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22)) + ((a & b) | (c & (a | b)));
+        const uint32_t t1 = add_fma(h, kw[i * S]) + sha_Sigma1(e) + ((e & f) ^ (~e & g));
+        const uint32_t t2 = sha_Sigma0(a) + ((a & b) | (c & (a | b)));
         h = g;
         g = f;
         f = e;

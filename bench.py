@@ -50,7 +50,7 @@ KEYGEN_CMP_128F = 4567   # top-layer XMSS tree: 8 leaves x 570 + 7 H
 
 
 def int_frac(signs, verifies, peak_ops):
-    """Fraction of the measured integer-ALU peak that `signs`/s and
+    """Fraction of the measured SHA-256-mix integer peak that `signs`/s and
     `verifies`/s of SHA-256-128f-simple amount to."""
     return (signs * SIGN_CMP_128F + verifies * VERIFY_CMP_128F) * OPS_PER_CMP / peak_ops
 
@@ -201,7 +201,10 @@ def main():
     eng = c.Engine(local)
     sid = c.set_id(SET)
     z = c.set_sizes(sid)
-    peak_ops, _ = c.int_peak(local, 8192)
+    # roofline denominators: the SHA-256 round's pipe mix (7 ALU : 1 FMA), and
+    # the ALU pipe alone (reported beside it)
+    peak_ops, _ = c.int_peak(local, 8192, mix=1)
+    peak_alu, _ = c.int_peak(local, 8192, mix=0)
     # per-set launch mapping for this batch shape (autotuner, cached per GPU)
     from cuspx_gb300 import autotune
     tuned = {"sign": autotune.tune(eng, sid, c.OP_SIGN, count=BATCH, mlen=MLEN)[0],
@@ -369,7 +372,9 @@ def main():
                          "traffic": traffic,
                          "work": "%d compressions x %d INT ops per launch" %
                                  (BATCH * 176 * LEAF_CMP[16], OPS_PER_CMP),
-                         "peak_source": "measured in this run: SHF/LOP3/IADD3 mix on all SMs (cuspx_int_peak)",
+                         "peak_source": "measured in this run on all SMs: SHA-256 round mix, 7 ALU ops "
+                                        "(SHF/LOP3/IADD3) to 1 IMAD on the FMA pipe (cuspx_int_peak_mix 1)",
+                         "peak_alu_only": peak_alu / 1e12,
                          "share_of_step": leaves / (tot / 3)},
             "clocks": ck,
             "wall_s_timed": wall,
@@ -627,9 +632,12 @@ def profile_case(count, setname):
     vv = np.zeros(count, dtype=np.int32)
     vb.download(None, None, vv)
     ok = bool((st == 0).all() and (vv == 0).all())
+    # the two roofline calibration kernels, short, after the batches, so a
+    # capture can read their pipe split next to the hash kernels'
+    peaks = {"int_peak_mix%d" % mix: round(c.int_peak(0, 256, mix=mix)[0] / 1e12, 3) for mix in (0, 1)}
     print(json.dumps({"profile_case": setname, "count": count, "ok": ok,
                       "sign_kernels_ms": {k: round(m, 3) for k, m, _ in sb.kernel_ms()},
-                      "verify_kernels_ms": {k: round(m, 3) for k, m, _ in vb.kernel_ms()}}))
+                      "verify_kernels_ms": {k: round(m, 3) for k, m, _ in vb.kernel_ms()}, **peaks}))
     sb.close(); vb.close(); eng.close()
     return 0 if ok else 1
 

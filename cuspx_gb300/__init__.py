@@ -27,7 +27,7 @@ EXPORTS = [
     "cuspx_batch_download", "cuspx_batch_sync", "cuspx_batch_last_ms", "cuspx_batch_stream",
     "cuspx_batch_device_ptrs", "cuspx_batch_profile", "cuspx_batch_kernel_ms",
     "cuspx_randombytes_init", "cuspx_randombytes", "cuspx_aes256_ecb", "cuspx_set_deterministic",
-    "cuspx_deterministic", "cuspx_int_peak",
+    "cuspx_deterministic", "cuspx_int_peak", "cuspx_int_peak_mix",
 ]
 
 
@@ -94,6 +94,7 @@ def lib():
     L.cuspx_set_deterministic.argtypes = [c.c_int]
     L.cuspx_set_deterministic.restype = None
     L.cuspx_int_peak.argtypes = [c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
+    L.cuspx_int_peak_mix.argtypes = [c.c_int, c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
     _lib = L
     return L
 
@@ -327,13 +328,14 @@ def set_deterministic(on):
     lib().cuspx_set_deterministic(1 if on else 0)
 
 
-def int_peak(device=0, iters=4096):
-    """Measured integer-ALU peak (ops/s) for the SHF/LOP3/IADD3 mix."""
+def int_peak(device=0, iters=4096, mix=0):
+    """Measured integer peak (ops/s): mix 0 the ALU-pipe SHF/LOP3/IADD3 shape
+    (Keccak-f), mix 1 a SHA-256 round with one add in eight on the FMA pipe."""
     ops = ctypes.c_double()
     ms = ctypes.c_float()
-    rc = lib().cuspx_int_peak(device, iters, ctypes.byref(ops), ctypes.byref(ms))
+    rc = lib().cuspx_int_peak_mix(device, iters, mix, ctypes.byref(ops), ctypes.byref(ms))
     if rc != 0:
-        raise CuspxError("cuspx_int_peak failed (%d)" % rc)
+        raise CuspxError("cuspx_int_peak_mix failed (%d)" % rc)
     return ops.value, ms.value
 
 

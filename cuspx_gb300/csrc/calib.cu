@@ -1,11 +1,15 @@
-// calib.cu -- integer-ALU peak microbenchmark (the roofline denominator).
+// calib.cu -- integer peak microbenchmarks (the roofline denominators).
 //
 // The hash cores are bound by 32-bit integer issue: funnel-shift rotates
-// (SHF), three-input logic (LOP3) and three-input adds (IADD3).  This kernel
-// issues that mix -- per step 3 SHF + 1 LOP3 + 1 IADD3, the shape of one
-// SHA-256 Sigma plus its add -- on eight independent chains per thread so
-// latency is hidden, at full occupancy on every SM.  ops/s = threads x
-// iterations x ops per iteration / elapsed.
+// (SHF), three-input logic (LOP3) and three-input adds (IADD3) on the ALU
+// pipe.  Mix 0 issues that shape alone -- per step 3 SHF + 1 LOP3 + 1 IADD3,
+// one SHA-256 Sigma plus its add -- which is also the Keccak-f shape (no
+// adds move off the ALU there).  Mix 1 is a SHA-256 round as the hash core
+// issues it: Sigma (3 SHF + LOP3), Ch (LOP3), a four-input add (2 IADD3) and
+// one add as IMAD on the FMA pipe (a * c_one + b with an opaque constant-bank
+// one), 7 ALU : 1 FMA like the compression's 1208 : 176.  Both run eight
+// independent chains per thread so latency is hidden, at full occupancy on
+// every SM.  ops/s = threads x iterations x chains x ops per step / elapsed.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -14,8 +18,9 @@
 namespace {
 
 constexpr int kChains = 8;
-constexpr int kOpsPerStep = 5;  // 3 SHF + LOP3 + IADD3
+__constant__ uint32_t c_calib_one = 1u;
 
+template <int MIX>
 __global__ void k_int_mix(uint32_t *out, int iters, uint32_t seed) {
     uint32_t x[kChains];
 #pragma unroll
@@ -25,7 +30,13 @@ __global__ void k_int_mix(uint32_t *out, int iters, uint32_t seed) {
         for (int c = 0; c < kChains; c++) {
             uint32_t v = x[c];
             uint32_t s = __funnelshift_r(v, v, 6) ^ __funnelshift_r(v, v, 11) ^ __funnelshift_r(v, v, 25);
-            x[c] = v + s + 0x428a2f98u + c;
+            if (MIX == 0) {
+                x[c] = v + s + 0x428a2f98u + c;
+            } else {
+                uint32_t y = x[(c + 1) % kChains], z = x[(c + 2) % kChains];
+                uint32_t t = v + s + ((v & y) ^ (~v & z)) + 0x428a2f98u;
+                x[c] = t * c_calib_one + (0x71374491u + c);
+            }
         }
     }
     uint32_t acc = 0;
@@ -36,20 +47,22 @@ __global__ void k_int_mix(uint32_t *out, int iters, uint32_t seed) {
 
 }  // namespace
 
-extern "C" int cuspx_int_peak(int device, int iters, double *ops_per_s, float *ms_out) {
-    if (!ops_per_s) return CUSPX_EINVAL;
+extern "C" int cuspx_int_peak_mix(int device, int iters, int mix, double *ops_per_s, float *ms_out) {
+    if (!ops_per_s || iters <= 0 || (mix != 0 && mix != 1)) return CUSPX_EINVAL;
     if (cudaSetDevice(device) != cudaSuccess) return CUSPX_ECUDA;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int threads = 256, blocks = sms * 8;
+    void (*kern)(uint32_t *, int, uint32_t) = mix ? k_int_mix<1> : k_int_mix<0>;
+    const int ops_per_step = mix ? 8 : 5;
     uint32_t *out = nullptr;
     if (cudaMalloc(&out, 4) != cudaSuccess) return CUSPX_ECUDA;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    k_int_mix<<<blocks, threads>>>(out, iters / 4 + 1, 1u);  // warm-up
+    kern<<<blocks, threads>>>(out, iters / 4 + 1, 1u);  // warm-up
     cudaEventRecord(e0);
-    k_int_mix<<<blocks, threads>>>(out, iters, 1u);
+    kern<<<blocks, threads>>>(out, iters, 1u);
     cudaEventRecord(e1);
     cudaError_t e = cudaEventSynchronize(e1);
     float ms = 0;
@@ -58,8 +71,12 @@ extern "C" int cuspx_int_peak(int device, int iters, double *ops_per_s, float *m
     cudaEventDestroy(e1);
     cudaFree(out);
     if (e != cudaSuccess) return CUSPX_ECUDA;
-    const double ops = (double)blocks * threads * iters * kChains * kOpsPerStep;
+    const double ops = (double)blocks * threads * iters * kChains * ops_per_step;
     *ops_per_s = ops / (ms * 1e-3);
     if (ms_out) *ms_out = ms;
     return CUSPX_OK;
+}
+
+extern "C" int cuspx_int_peak(int device, int iters, double *ops_per_s, float *ms_out) {
+    return cuspx_int_peak_mix(device, iters, 0, ops_per_s, ms_out);
 }

@@ -182,9 +182,13 @@ int cuspx_sign_noalloc(int set, size_t count, const uint8_t *d_sks, const uint8_
                        uint8_t *d_sigs, int32_t *d_status, void *stream);
 
 /* ---- calibration --------------------------------------------------------
- * Measured integer-ALU peak of this GPU for the hash cores' instruction mix
- * (funnel-shift rotate, 3-input logic, 3-input add) on all SMs at full
- * occupancy: the roofline denominator for the hash kernels. */
+ * Measured integer peak of this GPU on all SMs at full occupancy: the
+ * roofline denominator for the hash kernels.  mix 0: ALU pipe alone
+ * (funnel-shift rotate, 3-input logic, 3-input add; the Keccak-f shape);
+ * mix 1: a SHA-256 round as the hash core issues it, 7 ALU ops to one add
+ * on the FMA pipe.  cuspx_int_peak is mix 0.  No counterpart in the
+ * reference, which publishes no roofline. */
+int cuspx_int_peak_mix(int device, int iters, int mix, double *ops_per_s, float *ms);
 int cuspx_int_peak(int device, int iters, double *ops_per_s, float *ms);
 
 #ifdef __cplusplus

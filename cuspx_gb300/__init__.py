@@ -24,7 +24,7 @@ EXPORTS = [
     "cuspx_num_sets", "cuspx_set_id", "cuspx_set_name", "cuspx_set_sizes", "cuspx_create", "cuspx_destroy",
     "cuspx_error", "cuspx_set_tuning", "cuspx_get_tuning", "cuspx_keypair_batch", "cuspx_sign_batch",
     "cuspx_verify_batch", "cuspx_batch_create", "cuspx_batch_destroy", "cuspx_batch_upload", "cuspx_batch_run",
-    "cuspx_batch_download", "cuspx_batch_sync", "cuspx_batch_last_ms", "cuspx_batch_stream",
+    "cuspx_batch_download", "cuspx_batch_download_async", "cuspx_batch_sync", "cuspx_batch_last_ms", "cuspx_batch_stream",
     "cuspx_batch_device_ptrs", "cuspx_batch_profile", "cuspx_batch_kernel_ms",
     "cuspx_randombytes_init", "cuspx_randombytes", "cuspx_aes256_ecb", "cuspx_set_deterministic",
     "cuspx_deterministic", "cuspx_int_peak", "cuspx_int_peak_mix",
@@ -78,6 +78,7 @@ def lib():
     L.cuspx_batch_upload.argtypes = [vp, sz, vp, sz, vp, vp, sz, vp, vp, vp, vp]
     L.cuspx_batch_run.argtypes = [vp]
     L.cuspx_batch_download.argtypes = [vp, vp, vp, vp]
+    L.cuspx_batch_download_async.argtypes = [vp, vp, vp, vp]
     L.cuspx_batch_sync.argtypes = [vp]
     L.cuspx_batch_last_ms.argtypes = [vp, c.POINTER(c.c_float)]
     L.cuspx_batch_stream.argtypes = [vp]
@@ -281,6 +282,12 @@ class Batch:
 
     def download(self, out=None, out2=None, status=None):
         self.eng._check(self.L.cuspx_batch_download(self.h, _buf(out), _buf(out2), _buf(status)), "batch_download")
+
+    def download_async(self, out=None, out2=None, status=None):
+        """Enqueue the copies of download() on the batch stream without
+        waiting; the host buffers must be pinned and stay alive until sync()."""
+        self.eng._check(self.L.cuspx_batch_download_async(self.h, _buf(out), _buf(out2), _buf(status)),
+                        "batch_download_async")
 
     def sync(self):
         self.eng._check(self.L.cuspx_batch_sync(self.h), "batch_sync")

@@ -118,6 +118,7 @@ struct cuspx_batch {
     SetParams P{};
     size_t cap = 0, msg_cap = 0, key_cap = 0;
     cudaStream_t s = nullptr;
+    StreamFork fork{};         // sign batches: FORS beside the hypertree
     uint8_t *keys = nullptr;
     uint32_t *keyrow = nullptr;
     uint8_t *msg = nullptr;
@@ -382,6 +383,14 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
     cudaEventCreate(&b->e0);
     cudaEventCreate(&b->e1);
     for (auto &e : b->pt.ev) cudaEventCreate(&e);
+    if (op == CUSPX_OP_SIGN) {
+        if (cudaStreamCreateWithFlags(&b->fork.side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->fork.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->fork.join, cudaEventDisableTiming) != cudaSuccess) {
+            cuspx_batch_destroy(b);
+            return fail(ctx, CUSPX_ECUDA, "side stream");
+        }
+    }
     const size_t keyrow_bytes = op == CUSPX_OP_VERIFY ? 2 * n : 4 * n;
     A((void **)&b->keys, b->key_cap * keyrow_bytes);
     A((void **)&b->status, cap * sizeof(int32_t));
@@ -435,6 +444,12 @@ void cuspx_batch_destroy(cuspx_batch *b) {
     if (b->e1) cudaEventDestroy(b->e1);
     for (auto &e : b->pt.ev)
         if (e) cudaEventDestroy(e);
+    if (b->fork.side) {
+        cudaStreamSynchronize(b->fork.side);
+        cudaStreamDestroy(b->fork.side);
+    }
+    if (b->fork.fork) cudaEventDestroy(b->fork.fork);
+    if (b->fork.join) cudaEventDestroy(b->fork.join);
     if (b->s) cudaStreamDestroy(b->s);
     delete b;
 }
@@ -497,6 +512,11 @@ int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t
     return CUSPX_OK;
 }
 
+// FORS on a side stream beside the hypertree (0: one stream, for A/B runs)
+#ifndef CUSPX_SIGN_FORK
+#define CUSPX_SIGN_FORK 1
+#endif
+
 static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
     const FamilyOps &ops = family_of(b->set);
     const Tuning &tu = b->ctx->tune[b->set];
@@ -518,7 +538,8 @@ static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
         A.status = b->status;
         A.ends = b->ends;
         A.ends_cap = b->ends_cap;
-        ops.sign(P, A, tu, b->s, pt, b->long_msgs ? kPairMsgBytes : 0);
+        ops.sign(P, A, tu, b->s, pt, b->long_msgs ? kPairMsgBytes : 0,
+                 (CUSPX_SIGN_FORK && b->fork.side) ? &b->fork : nullptr);
     } else if (b->op == CUSPX_OP_VERIFY) {
         VerifyArgs A;
         A.count = cnt;
@@ -641,6 +662,7 @@ int cuspx_batch_sync(cuspx_batch *b) {
 int cuspx_batch_download_async(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status) {
     if (!b) return CUSPX_EINVAL;
     cuspx_ctx *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), ctx);
     const SetParams &P = b->P;
     const size_t cnt = b->count;
     if (!cnt) return CUSPX_OK;
@@ -657,7 +679,6 @@ int cuspx_batch_download_async(cuspx_batch *b, uint8_t *out, uint8_t *out2, int3
 
 int cuspx_batch_download(cuspx_batch *b, uint8_t *out, uint8_t *out2, int32_t *status) {
     if (!b) return CUSPX_EINVAL;
-    CK(cudaSetDevice(b->ctx->device), b->ctx);
     int rc = cuspx_batch_download_async(b, out, out2, status);
     if (rc) return rc;
     return cuspx_batch_sync(b);
@@ -682,7 +703,19 @@ namespace cuspx {
 // a long-message kernel) and holds the driver meanwhile, stalling every
 // thread's CUDA calls.  A direct launch of the 4-8 kernels costs tens of us.
 void batch_direct_launch(cuspx_batch *b, bool on) {
-    if (b) b->direct = on;
+    if (!b) return;
+    b->direct = on;
+    // Serving launches stay on one stream: with a second stream per sign
+    // slot the <= 1 KiB sign p99 of a mixed 16 B..1 MiB request stream rose
+    // from 2.5 to 17 ms (more streams than hardware queues, so short
+    // launches queue behind long ones).
+    if (on && b->fork.side) {
+        cudaStreamSynchronize(b->fork.side);
+        cudaStreamDestroy(b->fork.side);
+        cudaEventDestroy(b->fork.fork);
+        cudaEventDestroy(b->fork.join);
+        b->fork = StreamFork{};
+    }
 }
 
 // Library-internal: give an idle batch a stream of the given priority (lower
@@ -696,6 +729,12 @@ int batch_set_stream_priority(cuspx_batch *b, int priority) {
     b->graphs.clear();
     cudaStreamDestroy(b->s);
     b->s = ns;
+    if (b->fork.side) {   // the FORS side stream runs at the same priority
+        CK(cudaStreamSynchronize(b->fork.side), b->ctx);
+        CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, priority), b->ctx);
+        cudaStreamDestroy(b->fork.side);
+        b->fork.side = ns;
+    }
     return CUSPX_OK;
 }
 }  // namespace cuspx

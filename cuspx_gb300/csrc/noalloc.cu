@@ -110,6 +110,6 @@ extern "C" int cuspx_sign_noalloc(int set, size_t count, const uint8_t *d_sks, c
     base += up256(count * P.d * n);
     A.chains = base;
     Tuning tu;   // the default mapping: any mapping gives the same bytes
-    ops.sign(P, A, tu, (cudaStream_t)stream, nullptr, 0);
+    ops.sign(P, A, tu, (cudaStream_t)stream, nullptr, 0, nullptr);
     return cudaGetLastError() == cudaSuccess ? CUSPX_OK : CUSPX_ECUDA;
 }

@@ -167,11 +167,11 @@ static bool size_slot(cuspx_server *s, Group &g, Slot *sl) {
     const size_t cap = (size_t)s->cfg.max_batch;
     const size_t msg_cap = class_msg_bytes(s, g);
     if (cuspx_batch_create(s->ctx, g.op, g.set, cap, msg_cap, 1, &sl->b) != CUSPX_OK) return false;
+    batch_direct_launch(sl->b, true);   // no graph instantiation while serving
     // short-message launches run ahead of long-message ones on the GPU
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     batch_set_stream_priority(sl->b, g.long_class ? lo : hi);
-    batch_direct_launch(sl->b, true);   // no graph instantiation while serving
     const KeyTable &kt = s->keys[g.set];
     cuspx_batch_bind_keys(sl->b, g.op == CUSPX_OP_SIGN ? kt.d_sk : kt.d_pk, kt.cap);
     auto host = [](void **p, size_t bytes) { return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };

@@ -56,11 +56,23 @@ struct PhaseTimer {
         if (pt) (pt)->mark(name, s); \
     } while (0)
 
+// A side stream for the part of a sign sequence that runs beside the rest:
+// the FORS trees need only the message digest, and the hypertree leaves and
+// trees do not need FORS, so k_fors_sign runs on `side` between `fork`
+// (recorded after the message kernels) and `join` (waited before
+// k_sign_finish).  Works inside graph capture as a fork/join of the graph.
+struct StreamFork {
+    cudaStream_t side;
+    cudaEvent_t fork, join;
+};
+
 struct FamilyOps {
     cudaError_t (*configure)();
     // long_msg: messages of at least this many bytes are hashed two warps per
-    // 32 messages (SHA-256 sets; 0 or a SHAKE set: one thread each)
-    void (*sign)(const SetParams &, const SignArgs &, const Tuning &, cudaStream_t, PhaseTimer *, uint64_t long_msg);
+    // 32 messages (SHA-256 sets; 0 or a SHAKE set: one thread each).
+    // fk: optional side stream (ignored while per-kernel timing is on).
+    void (*sign)(const SetParams &, const SignArgs &, const Tuning &, cudaStream_t, PhaseTimer *, uint64_t long_msg,
+                 const StreamFork *fk);
     void (*verify)(const SetParams &, const VerifyArgs &, const Tuning &, cudaStream_t, PhaseTimer *,
                    uint64_t long_msg);
     void (*keygen)(const SetParams &, const KeygenArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
@@ -189,7 +201,7 @@ struct Family {
     }
 
     static void sign(const SetParams &P, const SignArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
-                     uint64_t long_msg) {
+                     uint64_t long_msg, const StreamFork *fk) {
         if (A.count == 0) return;
         if (HF::kShake) long_msg = 0;   // the two-warp message kernels are SHA-256 only
         k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A, long_msg);
@@ -200,6 +212,12 @@ struct Family {
                 CUSPX_MARK(pt, "k_sign_msg_pair", s);
             }
         }
+        const bool split = fk && !pt;
+        cudaStream_t sf = split ? fk->side : s;
+        if (split) {
+            cudaEventRecord(fk->fork, s);
+            cudaStreamWaitEvent(sf, fk->fork, 0);
+        }
         {
             const int b = tu.fors_block;
             // small batches: spread each tree over more lanes until the launch
@@ -207,9 +225,10 @@ struct Family {
             int g = tu.fors_lanes_log2 < P.a ? tu.fors_lanes_log2 : P.a;
             while (g < 5 && g < P.a && (((uint64_t)A.count * P.k) << g) < 152ull * 128) g++;
             const uint64_t threads = (((uint64_t)A.count * P.k) << g);
-            k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - g + 1) * W * 4, s>>>(P, A, g);
+            k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - g + 1) * W * 4, sf>>>(P, A, g);
             CUSPX_MARK(pt, "k_fors_sign", s);
         }
+        if (split) cudaEventRecord(fk->join, sf);
         {
             LeafArgs L{A.count, 0, P.d, A.sk, A.work, A.leaves, A.chains, A.ends};
             leaves(P, L, tu, s, pt, A.ends && A.count <= (uint32_t)tu.chain_mode_max && A.count <= A.ends_cap);
@@ -219,6 +238,7 @@ struct Family {
             trees(P, T, tu, s);
             CUSPX_MARK(pt, "k_trees", s);
         }
+        if (split) cudaStreamWaitEvent(s, fk->join, 0);
         k_sign_finish<HF><<<A.count, 128, (8 + HF::kSmemWords) * 4, s>>>(P, A);
         CUSPX_MARK(pt, "k_sign_finish", s);
     }

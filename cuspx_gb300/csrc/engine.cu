@@ -80,6 +80,9 @@ using namespace cuspx;
 // items per batch for which chain-parallel leaf scratch is allocated (the
 // largest chain_mode_max that can take effect)
 static const size_t kChainModeItems = 256;
+// keys per key-generation batch that the chain-parallel scratch covers
+// (16384 x 2^hp x len x n: 73 MB at 128f)
+static const size_t kKeygenChainItems = 16384;
 // messages of at least this many bytes (32 SHA-256 blocks) are hashed by the
 // two-warp message kernels of the SHA-256 sets
 static const uint64_t kPairMsgBytes = 2048;
@@ -398,8 +401,8 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
         A((void **)&b->out, cap * 2 * n);
         A((void **)&b->leaves, cap * ((size_t)1 << P.hp) * n);
         A((void **)&b->roots, cap * n);
-        // chain-parallel scratch for small key batches
-        b->ends_cap = (uint32_t)std::min<size_t>(cap, (size_t)kChainModeItems * P.d);
+        // chain-parallel scratch
+        b->ends_cap = (uint32_t)std::min<size_t>(cap, kKeygenChainItems);
         A((void **)&b->ends, (size_t)b->ends_cap * ((size_t)1 << P.hp) * P.len * n);
     } else {
         A((void **)&b->keyrow, cap * sizeof(uint32_t));

@@ -284,7 +284,11 @@ struct Family {
         if (K.count == 0) return;
         KeyRef kr{K.sk, nullptr, (uint32_t)(4 * N)};
         LeafArgs L{K.count, P.d - 1, 1, kr, nullptr, K.leaves, nullptr, K.ends};
-        leaves(P, L, tu, s, pt, K.ends && K.count <= (uint32_t)tu.chain_mode_max * P.d && K.count <= K.ends_cap);
+        // the top layer alone is 2^hp leaves per key, so one lane per leaf
+        // leaves SMs idle up to thousands of keys (4096 keys: 1.27 ms one
+        // lane per leaf, 1.17 ms one lane per chain); chain lanes whenever
+        // the scratch holds the batch, unless chain_mode_max is 0
+        leaves(P, L, tu, s, pt, K.ends && tu.chain_mode_max > 0 && K.count <= K.ends_cap);
         TreeArgs T{K.count, P.d - 1, 1, kr, nullptr, K.leaves, K.roots, nullptr};
         trees(P, T, tu, s);
         CUSPX_MARK(pt, "k_trees", s);

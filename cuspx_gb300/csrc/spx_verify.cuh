@@ -591,6 +591,10 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
     for (int i = 0; i < W; i++) v[i] = 0;
     typename PV::LaneRegs lr{};
     bool upkeep = true;   // a slot may be empty or waiting for its next layer
+    // warp-uniform: slots that may still have a chain or the T stream to hand
+    // out, so the claim loop reads nothing for the others (SHA-256-128f at
+    // 4096 items -2.3%, robust SHAKE-256f -8%)
+    uint32_t open = 0;
 
     while (true) {
         // ---- slot upkeep: refill empty slots, set up layers (warp-uniform) ----
@@ -639,6 +643,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                     S[PV::S_MASK] = S[PV::S_MASK + 1] = S[PV::S_MASK + 2] = ~0u;   // all roots present
                     S[PV::S_STATE] = PV::ACTIVE;
                 }
+                open |= 1u << g;
                 __syncwarp();
             }
             if (S[PV::S_STATE] == PV::ADVANCE) {
@@ -688,6 +693,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                     S[PV::S_MASK + 2] = PV::mask_init(2, LEN);
                     S[PV::S_STATE] = PV::ACTIVE;
                 }
+                open |= 1u << g;
                 __syncwarp();
             }
         }
@@ -696,9 +702,13 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         // ---- task claims (warp-uniform; slot order is priority order, and
         // within a slot the T stream -- the critical path -- comes first) ----
         uint32_t need = __ballot_sync(0xffffffffu, kind == PV::K_NONE);
-        for (int g = 0; g < G && need; g++) {
+        for (uint32_t om = open; om && need; om &= om - 1) {
+            const int g = __ffs(om) - 1;
             uint32_t *S = slots + g * SW;
-            if (S[PV::S_STATE] != PV::ACTIVE) continue;
+            if (S[PV::S_STATE] != PV::ACTIVE) {
+                open &= ~(1u << g);   // the upkeep sets it again
+                continue;
+            }
             // (a masked T starts at once: its mask stream needs no chain)
             if (S[PV::S_TCLAIM] == 0 &&
                 (PV::kTMask || PV::done_prefix(S) > PV::block_last_value(0, (int)S[PV::S_M]))) {
@@ -741,6 +751,10 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 __syncwarp();
                 need = __ballot_sync(0xffffffffu, kind == PV::K_NONE);
             }
+            // lanes still free: every chain of the slot is handed out; with
+            // the T stream taken too there is nothing more until the slot's
+            // next layer (set again by the upkeep)
+            if (need && S[PV::S_TCLAIM] != 0) open &= ~(1u << g);
         }
         if (!__any_sync(0xffffffffu, kind != PV::K_NONE)) break;
 
@@ -789,8 +803,9 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         if (run && step && kind == PV::K_CHAIN) {
             PV::value_out(u, v);
             if (++ts >= 15) {
+                // the T lane reads this value only after the __syncwarp that
+                // ends the iteration (slots are warp-private), so no fence
                 PV::write_value(S + PV::S_HDR, tc, v);
-                __threadfence_block();   // the end value is in the stream before its done bit
                 PV::mark_done(S, tc);
                 kind = PV::K_NONE;
             }

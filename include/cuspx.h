@@ -73,7 +73,9 @@ typedef struct {
     int fors_lanes_log2;  /* lanes per FORS tree = 2^g, g in 0..5 (0: lane per tree, 5: warp per tree) */
     int tree_mode;        /* 0 warp per XMSS subtree, 1 lane per subtree (heights <= 4 only) */
     int chain_mode_max;   /* batches of at most this many signatures (up to 256) compute XMSS
-                             leaves one lane per WOTS+ chain instead of one lane per leaf */
+                             leaves one lane per WOTS+ chain instead of one lane per leaf;
+                             key generation does so for batches of up to 16384 keys
+                             unless this is 0 */
     int verify_slots;     /* most items a warp holds at once in verify_mode 2 (1..8); batches
                              below about 4 warps per SM use fewer */
 } cuspx_tuning;

@@ -238,6 +238,27 @@ def test_sign_mappings_agree(engine, setname):
         engine.set_tuning(sid, **saved)
 
 
+def test_keygen_mappings_agree(engine):
+    """Key generation gives the same keys one lane per WOTS+ chain (taken for
+    any batch the chain scratch holds) and one lane per leaf (chain_mode_max
+    0), and they are the oracle's crypto_sign_seed_keypair keys."""
+    o = _oracle("sha256-128f-simple")
+    sid = engine.set_id("sha256-128f-simple")
+    rng = random.Random(53)
+    seeds = [bytes(rng.randrange(256) for _ in range(48)) for _ in range(300)]
+    saved = engine.get_tuning(sid)
+    try:
+        pks_c, sks_c = engine.keypair_batch(sid, seeds)
+        engine.set_tuning(sid, chain_mode_max=0)
+        pks_l, sks_l = engine.keypair_batch(sid, seeds)
+    finally:
+        engine.set_tuning(sid, **saved)
+    assert list(pks_c) == list(pks_l) and list(sks_c) == list(sks_l)
+    for i in (0, 157, 299):
+        pk, sk = o.seed_keypair(seeds[i])
+        assert pks_c[i] == pk and sks_c[i] == sk, i
+
+
 def test_mixed_sets_one_launch_vs_oracle(engine):
     """Uneven lengths, distinct keys and two parameter sets in one graph launch
     give the same signatures as the oracle item by item."""

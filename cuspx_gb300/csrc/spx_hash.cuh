@@ -133,6 +133,9 @@ SPX_DEV void sha256_iv(uint32_t s[8]) {
 
 // Rounds [R0, R1) of the compression on the working variables st = a..h;
 // w is the rolling 16-word schedule window (overwritten as it expands).
+// (Folding d into h + K + W a round early, e' = (d + h + K + W) + Sigma1 + Ch,
+// shortens the e chain by one step at one more ALU add a round; it measured
+// slower even for a warp alone on its SM: a lone verify 1.14 -> 1.20 ms.)
 template <int R0, int R1>
 SPX_DEV void sha256_rounds(uint32_t st[8], uint32_t w[16]) {
     uint32_t a = st[0], b = st[1], c = st[2], d = st[3], e = st[4], f = st[5], g = st[6], h = st[7];

@@ -683,8 +683,9 @@ def profile_case(count, setname):
 
 
 def plain_path(c):
-    """configs[0]: one keypair, 16 messages of 32..1024 B, keypair/sign/verify
-    one call at a time through the NIST api.h drop-in library."""
+    """The plain configuration: one keypair, 16 messages of 32..1024 B,
+    keypair/sign/verify one call at a time through the NIST api.h drop-in
+    library."""
     import ctypes
     import numpy as np
     L = ctypes.CDLL(c.dropin_path(SET))

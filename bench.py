@@ -41,8 +41,6 @@ BATCH = 4096
 MLEN = 64
 SUBSET = 64
 METRIC = "sign/s & verify/s, SHA2-128f, 1 GB300: batched+served vs plain; p50/p99 latency"
-# SHA-256 compressions per XMSS leaf for 128f (35 chains x (PRF + 15 F) + 10 T_len blocks)
-LEAF_CMP = {16: 35 * 16 + 10, 24: 51 * 16 + 20, 32: 67 * 16 + 36}
 OPS_PER_CMP = 1384   # INT ops of one SHA-256 compression (64 rounds x 14 + 48 x 10 + 8)
 # SHA-256 compressions per 128f operation, message hashing excluded (<1% at the
 # message lengths used here): sign = FORS + d x (2^hp leaves + tree) + T_k,
@@ -300,7 +298,7 @@ def main():
     tot = sum(m for _, m, _ in kern)
     leaves = [(m / n) for name, m, n in kern if name == "k_leaves"][0]
     P = dict(n=16, d=22, hp=3)
-    leaf_ops = BATCH * P["d"] * (1 << P["hp"]) * LEAF_CMP[P["n"]] * OPS_PER_CMP
+    leaf_ops = BATCH * P["d"] * (1 << P["hp"]) * leaf_units(SET) * OPS_PER_CMP
     achieved = leaf_ops / (leaves * 1e-3) / 1e12
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_leaves_sha256-128f_traffic.json")
@@ -377,6 +375,7 @@ def main():
     if rank == 0 and not args.no_extra:
         extra["uneven_mixed"] = uneven_mixed(c, eng)
         extra["verify_heavy"] = verify_heavy(c, eng)
+        extra["sign_sets_1024"] = sign_sets(c, eng, peak_alu, peak_ops)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -411,7 +410,7 @@ def main():
                          "peak": peak_ops / 1e12, "unit": "Tops/s", "frac": achieved / (peak_ops / 1e12),
                          "traffic": traffic,
                          "work": "%d compressions x %d INT ops per launch" %
-                                 (BATCH * 176 * LEAF_CMP[16], OPS_PER_CMP),
+                                 (BATCH * 176 * leaf_units(SET), OPS_PER_CMP),
                          "peak_source": "measured in this run on all SMs: SHA-256 round mix, 7 ALU ops "
                                         "(SHF/LOP3/IADD3) to 1 IMAD on the FMA pipe (cuspx_int_peak_mix 1)",
                          "peak_alu_only": peak_alu / 1e12,
@@ -537,6 +536,72 @@ def served_runs(c, eng, peak_ops, seconds=2.0):
     srv.close()
     out["served_stream"] = {"sets": names, "keys": per * len(sids), "lengths": "log-uniform 16 B..1 MiB",
                             "points": pts}
+    return out
+
+
+def leaf_units(name):
+    """Hash units (SHA-256 compressions or Keccak-f permutations) of one XMSS
+    leaf of a simple set: len chains of PRF + 15 F (one unit each at these
+    widths) and T_len over the len chain ends.  SHA-256 runs T_len after the
+    PUB_SEED midstate on ADRS_c (22 B) || values || padding (9 B min);
+    SHAKE-256 absorbs PUB_SEED || ADRS (32 B) || values at rate 136."""
+    n = {"128": 16, "192": 24, "256": 32}[name.split("-")[1][:3]]
+    ln = 2 * n + 3
+    if name.startswith("sha256"):
+        t = (22 + ln * n + 9 + 63) // 64
+    else:
+        t = (n + 32 + ln * n) // 136 + 1
+    return ln * 16 + t
+
+
+def sign_sets(c, eng, peak_alu, peak_mix, count=1024, mlen=256):
+    """Sign throughput of other simple sets at `count` signatures of `mlen`
+    random bytes (one key each, graph-launched batches), with k_leaves'
+    fraction of the integer peak for its hash: the SHA-256-round mix for
+    SHA-256, the ALU pipe alone for Keccak-f (which puts nothing on the FMA
+    pipe).  One signature per set is byte-compared with the CPU oracle."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+    hypertree = {"128f": (66, 22), "192f": (66, 22), "256f": (68, 17)}   # (h, d), params.h
+    out = {}
+    for name in ("sha256-192f-simple", "sha256-256f-simple", "shake256-128f-simple", "shake256-256f-simple"):
+        sid = c.set_id(name)
+        z = c.set_sizes(sid)
+        o = spx_oracle.Oracle(name)
+        rng = np.random.default_rng(123)
+        _, sks = eng.keypair_batch(sid, [rng.bytes(z["seed"])])
+        sk = bytes(sks[0])
+        msgs = rng.integers(0, 256, size=(count, mlen), dtype=np.uint8)
+        slab = np.ascontiguousarray(msgs.reshape(-1))
+        offs = np.arange(count, dtype=np.uint64) * mlen
+        lens = np.full(count, mlen, dtype=np.uint64)
+        kidx = np.zeros(count, dtype=np.uint32)
+        sb = eng.batch(c.OP_SIGN, sid, count, slab.nbytes, 1)
+        sb.upload(count, np.frombuffer(sk, dtype=np.uint8), 1, kidx, slab, slab.nbytes, offs, lens)
+        sb.run()
+        sigs = np.zeros(count * z["sig"], dtype=np.uint8)
+        sb.download(sigs)
+        ok = bytes(sigs[:z["sig"]]) == o.sign(bytes(msgs[0]), sk)
+        sb.run(); sb.sync()
+        ms = []
+        for _ in range(2):
+            sb.run(); sb.sync(); ms.append(sb.last_ms())
+        sb.profile(True)
+        sb.run(); sb.sync()
+        km = {k: m / n for k, m, n in sb.kernel_ms()}
+        sb.profile(False)
+        sb.close()
+        h, d = hypertree[name.split("-")[1]]
+        units = count * d * (1 << (h // d)) * leaf_units(name)
+        shake = name.startswith("shake")
+        ops = units * (4560 if shake else OPS_PER_CMP)
+        leaves = km.get("k_leaves")
+        peak = peak_alu if shake else peak_mix
+        out[name] = {"sign_per_s": count / (min(ms) / 1e3), "ms_per_batch": min(ms),
+                     "k_leaves_ms": leaves,
+                     "k_leaves_frac": ops / (leaves * 1e-3) / peak if leaves else None,
+                     "peak": "alu_only" if shake else "sha256_mix", "oracle_first_sig_agrees": ok}
     return out
 
 

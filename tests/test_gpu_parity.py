@@ -238,6 +238,40 @@ def test_sign_mappings_agree(engine, setname):
         engine.set_tuning(sid, **saved)
 
 
+def test_empty_batches_and_length_edges(engine):
+    """Zero-item keygen, sign and verify calls and batch runs return at once
+    with empty results; in a verify batch an empty message verifies like any
+    other, and a signature of length 0, SPX_BYTES - 1 or SPX_BYTES + 1 is
+    rejected (crypto_sign_verify, sign.cu:3064: siglen != SPX_BYTES -> -1)
+    without disturbing its neighbours."""
+    import cuspx_gb300 as c
+    for name in ("sha256-128f-simple", "shake256-128f-simple"):
+        o = _oracle(name)
+        sid = engine.set_id(name)
+        z = c.set_sizes(sid)
+        pks, sks = engine.keypair_batch(sid, [])
+        assert pks == [] and sks == []
+        sigs, st = engine.sign_batch(sid, [], [])
+        assert sigs == [] and len(st) == 0
+        assert len(engine.verify_batch(sid, [], [], [])) == 0
+        b = engine.batch(c.OP_SIGN, sid, 4, 64, 1)
+        b.upload(0, None)
+        b.run()
+        b.sync()
+        b.close()
+        rng = random.Random(8)
+        pk, sk = o.seed_keypair(bytes(rng.randrange(256) for _ in range(z["seed"])))
+        msgs = [b"", b"x" * 33]
+        sigs, st = engine.sign_batch(sid, [sk] * 2, msgs)
+        assert list(st) == [0, 0]
+        assert sigs[0] == o.sign(b"", sk) and sigs[1] == o.sign(msgs[1], sk)
+        vm = [msgs[0], msgs[1], msgs[0], msgs[1], msgs[0]]
+        vs = [sigs[0], sigs[1], b"", sigs[1], sigs[0]]
+        vl = [z["sig"], z["sig"], 0, z["sig"] - 1, z["sig"] + 1]
+        got = engine.verify_batch(sid, [pk] * 5, vm, vs, siglens=vl)
+        assert list(got) == [0, 0, -1, -1, -1]
+
+
 def test_keygen_mappings_agree(engine):
     """Key generation gives the same keys one lane per WOTS+ chain (taken for
     any batch the chain scratch holds) and one lane per leaf (chain_mode_max

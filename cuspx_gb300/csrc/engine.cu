@@ -242,11 +242,12 @@ int cuspx_create(int device, cuspx_ctx **out) {
         t.tree_mode = sd.h / sd.d <= 4 ? 1 : 0;
         t.leaf_block = (sd.hash == 0 && !sd.robust) ? 256 : 128;
         t.chains_per_warp = sd.hash == 1 ? 256 : 128;
-        t.verify_mode = (sd.robust && sd.hash == 0) ? 0 : 2;
-        // a robust SHAKE item is two units per F and H: fewer items per warp
+        t.verify_mode = 2;
+        // a robust item is several units per F and H: fewer items per warp
         // keep enough warps busy (16384 SHAKE-256f-robust: 2 slots 93.9 ms,
-        // 4 slots 98.9 ms)
-        if (sd.robust && sd.hash == 1) t.verify_slots = 2;
+        // 4 slots 98.9 ms; 4096 SHA-256-192f-robust 11.9 / 12.8 ms), except
+        // robust SHA-256 at n = 32 (4096 SHA-256-256f-robust 22.8 / 21.1 ms)
+        if (sd.robust && !(sd.hash == 0 && sd.n == 32)) t.verify_slots = 2;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;

@@ -19,8 +19,8 @@
 //
 // Verify: k_verify_msg (+ k_verify_msg_pair) -> k_verify_fors -> the
 // hypertree, either one persistent launch (k_verify_hyper, spx_verify.cuh;
-// the default for simple sets) or per-layer k_verify_chains + k_verify_root
-// (robust sets), or k_verify_ht (one thread per item over all layers).
+// the default) or per-layer k_verify_chains + k_verify_root, or k_verify_ht
+// (one thread per item over all layers).
 // Key generation reuses k_leaves / k_trees on the top layer.
 //
 // Reference structure followed (CPU form): crypto_sign_signature sign.cu:1924-1994,

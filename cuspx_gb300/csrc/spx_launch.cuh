@@ -19,7 +19,7 @@ struct Tuning {
     int tree_warps = 4;      // warps per block for k_trees (upper bound)
     int chains_per_warp = 64;  // (item, chain) tasks per warp in k_verify_chains
     int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers,
-                             // 2 persistent hypertree kernel (simple sets)
+                             // 2 persistent hypertree kernel
     int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
@@ -133,9 +133,10 @@ struct Family {
         return cudaSuccess;
     }
 
-    // the persistent verify kernel covers the simple sets of both hashes and
-    // the robust SHAKE-256 sets
-    static constexpr bool kPersistVerify = !HF::kRobust || HF::kShake;
+    // the persistent verify kernel covers every set (the robust SHA-256
+    // policy lays its slot out for subtrees of height <= 9, the tallest of
+    // any set)
+    static constexpr bool kPersistVerify = true;
 
     // one launch over the batch's whole hypertree: as many blocks as are
     // resident at once (or fewer for small batches); warps take items from
@@ -258,7 +259,7 @@ struct Family {
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_verify_fors", s);
         const int b = tu.verify_block;
-        if (tu.verify_mode == 2 && kPersistVerify && A.ctr) {
+        if (tu.verify_mode == 2 && kPersistVerify && A.ctr && P.hp <= 9) {
             verify_persistent(P, A, tu, s, pt);
             return;
         }

@@ -1,4 +1,4 @@
-// spx_verify.cuh -- persistent hypertree verify for the simple sets.
+// spx_verify.cuh -- persistent hypertree verify (every parameter set).
 //
 // crypto_sign_verify (sign.cu:3048-3121) is serial over the d layers of an
 // item: layer L's WOTS+ chains (wots_pk_from_sig, wots.cu:777-804) need the
@@ -267,7 +267,8 @@ struct VerifySha2 : VerifySlot<4 * HF::W, 22, 64> {
 #pragma unroll
         for (int i = 0; i < 8; i++) r.tst[i] = u.out[i];
     }
-    SPX_DEV static void after_h_first(const Unit &u, LaneRegs &r) {
+    // first block of a two-block H (the only H unit before the last)
+    SPX_DEV static void after_h_unit(const Unit &u, LaneRegs &r, int) {
 #pragma unroll
         for (int i = 0; i < 8; i++) r.tst[i] = u.out[i];
     }
@@ -408,7 +409,7 @@ struct VerifyShake : VerifySlot<4 * HF::W, 4 * HF::W + 32, 136> {
 #pragma unroll
         for (int i = 0; i < 25; i++) T[i] = u.A[i];
     }
-    SPX_DEV static void after_h_first(const Unit &, LaneRegs &) {}
+    SPX_DEV static void after_h_unit(const Unit &, LaneRegs &, int) {}
 };
 
 // ---------------------------------------------------------------------------
@@ -471,7 +472,7 @@ struct VerifyShakeRobust : VerifyShake<HF> {
             u.A[kPreLanes + NL] = 0x1Full;
         }
     }
-    SPX_DEV static void after_f_first(const Unit &u, LaneRegs &r) {
+    SPX_DEV static void after_f_unit(const Unit &u, LaneRegs &r, int) {
 #pragma unroll
         for (int i = 0; i < NL; i++) r.mk[i] = u.A[i];
     }
@@ -501,7 +502,7 @@ struct VerifyShakeRobust : VerifyShake<HF> {
             u.A[kPreLanes + 2 * NL] ^= 0x1Full;
         }
     }
-    SPX_DEV static void after_h_first(const Unit &u, LaneRegs &r) {
+    SPX_DEV static void after_h_unit(const Unit &u, LaneRegs &r, int) {
 #pragma unroll
         for (int i = 0; i < 2 * NL; i++) r.mk[i] = u.A[i];
     }
@@ -561,10 +562,240 @@ struct VerifyShakeRobust : VerifyShake<HF> {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Robust SHA-256: every thash input is xored with MGF1-SHA256(PUB_SEED ||
+// ADRS_c) before it is hashed (Sha2::thash).  A mask block is
+// SHA256(PUB_SEED || ADRS_c || BE32(ctr)) from the IV -- one compression for
+// n <= 24, two for n = 32 (kMB units).  A chain step is kMB mask units, then
+// the F unit on the masked value; an H is its ceil(2n / 32) mask blocks, then
+// its kHBlocks blocks on the masked l || r.  The T lane is claimed as soon as
+// its layer starts and computes the T mask (ceil(m n / 32) blocks) into a
+// second stream laid out byte for byte like the value stream and zero outside
+// the values, while the chains run; block j of T is absorbed with the mask
+// stream xored in once its chains and its mask bytes are there.
+// ---------------------------------------------------------------------------
+template <class HF>
+struct VerifySha2Robust : VerifySha2<HF> {
+    using S0 = VerifySha2<HF>;
+    using B = typename S0::B;
+    using Unit = typename S0::Unit;
+    static constexpr int W = S0::W, N = S0::N, LEN = S0::LEN;
+    static constexpr int kStreamWords = S0::kStreamWords;
+    static constexpr int kHBlocks = S0::kHBlocks;
+    static constexpr int kMaxHp = 9;                        // tallest subtree of any set
+    static constexpr int kMaskTot = N + 26;                 // PUB_SEED || ADRS_c || BE32(ctr)
+    static constexpr int kMB = (kMaskTot + 9 + 63) / 64;    // compressions per mask block
+    static constexpr int kHMaskBlocks = (2 * N + 31) / 32;
+    static constexpr int kFUnits = kMB + 1, kHUnits = kHMaskBlocks * kMB + kHBlocks;
+    static constexpr bool kTMask = true;
+    enum : int { S_MB = 14 };                               // header: T mask units done
+    // after the auth path (sized for kMaxHp): PUB_SEED (W big-endian words),
+    // the first-compression state of a T mask block (n = 32), the mask stream
+    static constexpr int kPub = B::S_HDR + kStreamWords + kMaxHp * W;
+    static constexpr int kMst = kPub + W;
+    static constexpr int kMStream = kMst + 8;
+    static __host__ __device__ int slot_words(int) { return kMStream + kStreamWords; }
+
+    struct LaneRegs : S0::LaneRegs {
+        uint32_t mk[2 * W];   // the current F or H mask
+    };
+
+    SPX_DEV static void load_key(uint32_t *S, const SignWork *wk, const uint8_t *pk, uint32_t lane) {
+        S0::load_key(S, wk, pk, lane);
+        if (lane < W) S[kPub + lane] = bswap32(reinterpret_cast<const uint32_t *>(pk)[lane]);
+    }
+    // the value stream's frame, and a zero mask stream
+    SPX_DEV static void frame(uint32_t *stream, const uint32_t *S, const Adrs &a, int m, uint32_t lane) {
+        S0::frame(stream, S, a, m, lane);
+        uint32_t *ms = stream + (kMStream - B::S_HDR);
+        for (int q = (int)lane; q < kStreamWords; q += 32) ms[q] = 0;
+    }
+    SPX_DEV static void claim_t(LaneRegs &r, uint32_t *S, int hp) {
+        S0::claim_t(r, S, hp);
+        S[S_MB] = 0;
+    }
+
+    // unit `part` of mask block `ctr` for ADRS words aw (part > 0 resumes
+    // from `prev`, the state after the block's first compression)
+    SPX_DEV static void mask_unit(Unit &u, const uint32_t *S, const uint32_t aw[6], uint32_t ctr, int part,
+                                  const uint32_t prev[8]) {
+        if (part == 0) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) u.st[i] = sha256_iv_word(i);
+#pragma unroll
+            for (int i = 0; i < W; i++) u.blk[i] = S[kPub + i];
+#pragma unroll
+            for (int i = 0; i < 5; i++) u.blk[W + i] = aw[i];
+            u.blk[W + 5] = (aw[5] & 0xffff0000u) | (ctr >> 16);
+            u.blk[W + 6] = (ctr << 16) | 0x8000u;
+#pragma unroll
+            for (int i = W + 7; i < 16; i++) u.blk[i] = 0;
+            if (kMB == 1) u.blk[15] = kMaskTot * 8;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; i++) u.st[i] = prev[i];
+#pragma unroll
+            for (int i = 0; i < 15; i++) u.blk[i] = 0;
+            u.blk[15] = kMaskTot * 8;
+        }
+    }
+
+    SPX_DEV static void build_chain(Unit &u, const LaneRegs &r, const uint32_t *S, int c, int s, int sub,
+                                    const uint32_t v[W]) {
+        if (sub < kMB) {
+            const uint32_t aw[6] = {S[B::S_AW0], S[B::S_AW1], S[B::S_AW2], S[B::S_IDXL] << 16,
+                                    (uint32_t)c << 16, (uint32_t)s << 16};
+            mask_unit(u, S, aw, 0, sub, r.tst);
+        } else {
+            uint32_t x[W];
+#pragma unroll
+            for (int i = 0; i < W; i++) x[i] = v[i] ^ r.mk[i];
+            S0::build_chain(u, r, S, c, s, 0, x);
+        }
+    }
+    SPX_DEV static void after_f_unit(const Unit &u, LaneRegs &r, int sub) {
+        if (sub < kMB - 1) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) r.tst[i] = u.out[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < W; i++) r.mk[i] = u.out[i];
+        }
+    }
+
+    // H of compute_root at height h -> h + 1 for node index idx; sub: mask
+    // units first, then the H blocks
+    SPX_DEV static void build_h(Unit &u, const LaneRegs &r, const uint32_t *S, int h, int sub, uint32_t idx,
+                                const uint32_t v[W], int) {
+        Adrs a;
+        a.w[0] = S[B::S_AW0];
+        a.w[1] = S[B::S_AW1];
+        a.w[2] = (S[B::S_AW2] & 0xff000000u) | (ADDR_HASHTREE << 16);
+        a.w[3] = 0;
+        a.w[4] = 0;
+        a.w[5] = 0;
+        adrs_height(a, h + 1);
+        adrs_index(a, idx >> 1);
+        constexpr int KM = kHMaskBlocks * kMB;
+        if (sub < KM) {
+            mask_unit(u, S, a.w, (uint32_t)(sub / kMB), sub % kMB, r.tst);
+            return;
+        }
+        const uint32_t *auth = S + B::S_HDR + kStreamWords + h * W;
+        const bool right = idx & 1u;
+        uint32_t in[2 * W];
+#pragma unroll
+        for (int i = 0; i < W; i++) {
+            const uint32_t sib = __byte_perm(auth[i], 0, 0x0123);
+            in[i] = (right ? sib : v[i]) ^ r.mk[i];
+            in[W + i] = (right ? v[i] : sib) ^ r.mk[W + i];
+        }
+        constexpr int TOT = 22 + 2 * N;
+        uint32_t m[16 * kHBlocks];
+#pragma unroll
+        for (int i = 0; i < 5; i++) m[i] = a.w[i];
+        m[5] = (a.w[5] & 0xffff0000u) | (in[0] >> 16);
+#pragma unroll
+        for (int i = 1; i < 2 * W; i++) m[5 + i] = __funnelshift_l(in[i], in[i - 1], 16);
+        m[5 + 2 * W] = (in[2 * W - 1] << 16) | 0x8000u;
+#pragma unroll
+        for (int i = 6 + 2 * W; i < 16 * kHBlocks; i++) m[i] = 0;
+        m[16 * kHBlocks - 1] = (64 + TOT) * 8;
+        if (kHBlocks == 1 || sub == KM) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) u.st[i] = r.kmid[i];
+#pragma unroll
+            for (int i = 0; i < 16; i++) u.blk[i] = m[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; i++) u.st[i] = r.tst[i];
+#pragma unroll
+            for (int i = 0; i < 16; i++) u.blk[i] = m[16 * (kHBlocks - 1) + i];
+        }
+    }
+    SPX_DEV static void after_h_unit(const Unit &u, LaneRegs &r, int sub) {
+        constexpr int KM = kHMaskBlocks * kMB;
+        if (sub < KM && sub % kMB == kMB - 1) {
+            // mask block sub / kMB: mask words 8b .. 8b + 7 (indices kept
+            // compile-time so mk stays in registers)
+#pragma unroll
+            for (int b = 0; b < kHMaskBlocks; b++)
+                if (b == sub / kMB) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++)
+                        if (8 * b + i < 2 * W) r.mk[8 * b + i] = u.out[i];
+                }
+        } else {
+            // a mask block's first compression, or the first of two H blocks
+#pragma unroll
+            for (int i = 0; i < 8; i++) r.tst[i] = u.out[i];
+        }
+    }
+
+    // T lane's next unit for block j: 1 = a mask unit (needed by block j, or
+    // ahead of the chains), 0 = block j, 2 = nothing ready
+    SPX_DEV static int t_action(const uint32_t *S, int j) {
+        const int m = (int)S[B::S_M];
+        const int done = (int)S[S_MB] / kMB;                 // complete mask blocks
+        const int hi = 64 * j + 41;                           // last value byte block j reads
+        const int last = hi < m * N - 1 ? hi : m * N - 1;
+        const int need = last / 32 + 1;
+        if (done < need) return 1;
+        if (B::done_prefix(S) > B::block_last_value(j, m)) return 0;
+        return done < (m * N + 31) / 32 ? 1 : 2;
+    }
+    SPX_DEV static void build_mask(Unit &u, uint32_t *S, int) {
+        const int units = (int)S[S_MB];
+        const uint32_t *st = S + B::S_HDR;   // the T ADRS_c, in memory order
+        uint32_t aw[6];
+#pragma unroll
+        for (int i = 0; i < 5; i++) aw[i] = bswap32(st[i]);
+        aw[5] = bswap32(st[5]) & 0xffff0000u;
+        uint32_t prev[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) prev[i] = S[kMst + i];
+        mask_unit(u, S, aw, (uint32_t)(units / kMB), units % kMB, prev);
+    }
+    // `nw` big-endian words at mask-stream byte `off` (2 mod 4), like write_value
+    SPX_DEV static void write_mask(uint32_t *base, int off, const uint32_t w[8], int nw) {
+        S0::put16(base, off, __byte_perm(w[0], 0, 0x0023));
+#pragma unroll
+        for (int i = 0; i < 7; i++)
+            if (i + 1 < nw) base[(off + 2) / 4 + i] = __byte_perm(w[i], w[i + 1], 0x6701);
+        uint32_t lastw = w[0];
+#pragma unroll
+        for (int i = 1; i < 8; i++)
+            if (i == nw - 1) lastw = w[i];
+        S0::put16(base, off + 4 * nw - 2, __byte_perm(lastw, 0, 0x0001));
+    }
+    SPX_DEV static void after_mask(const Unit &u, uint32_t *S, int) {
+        const int units = (int)S[S_MB];
+        const int b = units / kMB;
+        if (units % kMB < kMB - 1) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) S[kMst + i] = u.out[i];
+        } else {
+            const int m = (int)S[B::S_M];
+            const int left = m * N - 32 * b;                  // mask bytes still to place (> 0)
+            write_mask(S + kMStream, 22 + 32 * b, u.out, (left < 32 ? left : 32) / 4);
+        }
+        S[S_MB] = (uint32_t)(units + 1);
+    }
+    // T block j with its value bytes xored with the mask stream
+    SPX_DEV static void build_t(Unit &u, const LaneRegs &r, uint32_t *S, int j, int) {
+        const uint32_t *b = S + B::S_HDR + j * 16;
+        const uint32_t *mb = S + kMStream + j * 16;
+#pragma unroll
+        for (int i = 0; i < 8; i++) u.st[i] = r.tst[i];
+#pragma unroll
+        for (int i = 0; i < 16; i++) u.blk[i] = __byte_perm(b[i] ^ mb[i], 0, 0x0123);
+    }
+};
+
 template <class HF>
 using VerifyPolicy = typename std::conditional<
     HF::kShake != 0, typename std::conditional<HF::kRobust, VerifyShakeRobust<HF>, VerifyShake<HF>>::type,
-    VerifySha2<HF>>::type;
+    typename std::conditional<HF::kRobust, VerifySha2Robust<HF>, VerifySha2<HF>>::type>::type;
 
 template <class HF>
 __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A, uint32_t *ctr, int G) {
@@ -787,11 +1018,11 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         // ---- use the output ----
         bool slot_event = false;
         bool step = true;   // the chain step's last unit ran
-        if constexpr (PV::kFUnits == 2) {
+        if constexpr (PV::kFUnits > 1) {
             if (run && kind == PV::K_CHAIN) {
-                if (tsub == 0) PV::after_f_first(u, lr);
-                step = tsub == 1;
-                tsub ^= 1;
+                step = tsub == PV::kFUnits - 1;
+                if (!step) PV::after_f_unit(u, lr, tsub);
+                tsub = step ? 0 : tsub + 1;
             }
         }
         if constexpr (PV::kTMask) {
@@ -828,9 +1059,9 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 }
             }
         } else if (run && kind == PV::K_ROOT) {
-            if (PV::kHUnits == 2 && ts == 0) {
-                PV::after_h_first(u, lr);
-                ts = 1;
+            if (ts < PV::kHUnits - 1) {
+                PV::after_h_unit(u, lr, ts);
+                ts++;
             } else {
                 PV::value_out(u, v);
                 ts = 0;

@@ -68,8 +68,7 @@ typedef struct {
     int tree_warps;       /* warps per block, XMSS tree kernel */
     int chains_per_warp;  /* (item, chain) tasks per warp, verify chain kernel */
     int verify_mode;      /* 0 layered verify kernels, 1 one thread per item over all layers,
-                             2 one persistent launch over the whole hypertree (simple sets and
-                             robust SHAKE-256 sets; robust SHA-256 sets run 0 when 2 is asked for) */
+                             2 one persistent launch over the whole hypertree (default) */
     int fors_lanes_log2;  /* lanes per FORS tree = 2^g, g in 0..5 (0: lane per tree, 5: warp per tree) */
     int tree_mode;        /* 0 warp per XMSS subtree, 1 lane per subtree (heights <= 4 only) */
     int chain_mode_max;   /* batches of at most this many signatures (up to 256) compute XMSS

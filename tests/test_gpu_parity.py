@@ -135,7 +135,8 @@ def test_sign_status_flags_bad_key(engine):
 @pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-simple", "sha256-192f-robust",
                                      "sha256-192f-simple", "sha256-256f-simple", "sha256-128s-simple",
                                      "shake256-128f-simple", "shake256-192s-simple", "shake256-256f-robust",
-                                     "shake256-128f-robust", "shake256-192s-robust"])
+                                     "shake256-128f-robust", "shake256-192s-robust", "sha256-128f-robust",
+                                     "sha256-256f-robust", "sha256-128s-robust"])
 def test_verify_mappings_agree(engine, setname):
     """Every verify launch mapping the autotuner may pick returns the same verdicts."""
     o = _oracle(setname)

@@ -95,6 +95,8 @@ struct cuspx_ctx {
     std::mutex mu;       // one-shot batches
     std::mutex cfg_mu;   // kernel attribute configuration
     cuspx_batch *oneshot[3][kNumSets] = {};
+    uint8_t *stage = nullptr;   // pinned staging of the one-shot calls (under mu)
+    size_t stage_cap = 0;
     // multi-batch (mixed parameter set) graphs
     struct GroupGraph {
         std::vector<cuspx_batch *> batches;
@@ -253,6 +255,11 @@ int cuspx_create(int device, cuspx_ctx **out) {
         delete c;
         return CUSPX_ECUDA;
     }
+    // the one-shot calls' pinned staging, so that the first call does not
+    // pay for the allocation (it grows on demand for larger batches)
+    if (cudaMallocHost((void **)&c->stage, (size_t)1 << 20) == cudaSuccess) c->stage_cap = (size_t)1 << 20;
+    else c->stage = nullptr;
+    cudaGetLastError();
     *out = c;
     return CUSPX_OK;
 }
@@ -269,6 +276,7 @@ void cuspx_destroy(cuspx_ctx *ctx) {
     for (auto &row : ctx->oneshot)
         for (auto *b : row)
             if (b) cuspx_batch_destroy(b);
+    if (ctx->stage) cudaFreeHost(ctx->stage);
     delete ctx;
 }
 
@@ -806,19 +814,57 @@ static int oneshot_batch(cuspx_ctx *ctx, int op, int set, size_t count, size_t m
     return CUSPX_OK;
 }
 
-// pack messages at 16-byte aligned offsets
-static size_t pack_msgs(size_t count, const uint8_t *msgs, const uint64_t *off, const uint64_t *len,
-                        std::vector<uint8_t> &slab, std::vector<uint64_t> &noff) {
-    size_t total = 0;
-    noff.resize(count);
-    for (size_t i = 0; i < count; i++) {
-        noff[i] = total;
-        total += (len[i] + 15) & ~(uint64_t)15;
+static size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Pinned host staging for the one-shot calls (under ctx->mu): their inputs
+// are packed here and their outputs land here, so every copy is a direct
+// DMA rather than a pass through the driver's pageable bounce buffer (a
+// plain one-signature call makes six small copies).  Grown on demand and
+// kept for the context's life.
+struct Staging {
+    uint8_t *base = nullptr;
+    size_t used = 0;
+    void *take(size_t bytes) {
+        void *p = base + used;
+        used += al16(bytes);
+        return p;
     }
-    slab.assign(total + 16, 0);
-    for (size_t i = 0; i < count; i++)
-        if (len[i]) memcpy(slab.data() + noff[i], msgs + off[i], len[i]);
+};
+static int oneshot_stage(cuspx_ctx *ctx, size_t bytes, Staging &st) {
+    if (ctx->stage_cap < bytes) {
+        if (ctx->stage) cudaFreeHost(ctx->stage);
+        ctx->stage = nullptr;
+        ctx->stage_cap = 0;
+        const size_t cap = std::max<size_t>(bytes, (size_t)1 << 20);
+        if (cudaMallocHost((void **)&ctx->stage, cap) != cudaSuccess) {
+            ctx->stage = nullptr;
+            cudaGetLastError();
+            return fail(ctx, CUSPX_ECUDA, "cudaMallocHost: one-shot staging");
+        }
+        ctx->stage_cap = cap;
+    }
+    st.base = ctx->stage;
+    st.used = 0;
+    return CUSPX_OK;
+}
+// bytes of the messages packed at 16-byte aligned offsets
+static size_t packed_bytes(size_t count, const uint64_t *len) {
+    size_t total = 0;
+    for (size_t i = 0; i < count; i++) total += al16(len[i]);
     return total;
+}
+// pack the messages into staging: slab (total + 16 bytes, zero padding),
+// offsets and lengths
+static void pack_staged(size_t count, const uint8_t *msgs, const uint64_t *off, const uint64_t *len, size_t total,
+                        uint8_t *slab, uint64_t *noff, uint64_t *nlen) {
+    memset(slab, 0, total + 16);
+    size_t o = 0;
+    for (size_t i = 0; i < count; i++) {
+        noff[i] = o;
+        nlen[i] = len[i];
+        if (len[i]) memcpy(slab + o, msgs + off[i], len[i]);
+        o += al16(len[i]);
+    }
 }
 
 int cuspx_keypair_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *seeds, uint8_t *pks, uint8_t *sks) {
@@ -829,10 +875,21 @@ int cuspx_keypair_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *se
     cuspx_batch *b;
     int rc = oneshot_batch(ctx, CUSPX_OP_KEYGEN, set, count, 0, &b);
     if (rc) return rc;
-    if ((rc = cuspx_batch_upload(b, count, seeds, count, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr)))
+    const SetParams &P = b->P;
+    const size_t seed_b = count * 3 * P.n, sk_b = count * P.sk_bytes, pk_b = count * P.pk_bytes;
+    Staging st;
+    if ((rc = oneshot_stage(ctx, al16(seed_b) + al16(sk_b) + al16(pk_b), st))) return rc;
+    uint8_t *h_seed = (uint8_t *)st.take(seed_b);
+    uint8_t *h_sk = (uint8_t *)st.take(sk_b);
+    uint8_t *h_pk = (uint8_t *)st.take(pk_b);
+    memcpy(h_seed, seeds, seed_b);
+    if ((rc = cuspx_batch_upload(b, count, h_seed, count, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr)))
         return rc;
     if ((rc = cuspx_batch_run(b))) return rc;
-    return cuspx_batch_download(b, sks, pks, nullptr);
+    if ((rc = cuspx_batch_download(b, h_sk, h_pk, nullptr))) return rc;
+    memcpy(sks, h_sk, sk_b);
+    memcpy(pks, h_pk, pk_b);
+    return CUSPX_OK;
 }
 
 int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, const uint8_t *msgs,
@@ -842,20 +899,33 @@ int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, 
     if (count == 0) return CUSPX_OK;
     if (!sks || !msg_off || !msg_len || !sigs) return fail(ctx, CUSPX_EINVAL, "sign_batch: null buffer");
     std::lock_guard<std::mutex> lk(ctx->mu);
-    std::vector<uint8_t> slab;
-    std::vector<uint64_t> noff;
-    size_t total = pack_msgs(count, msgs, msg_off, msg_len, slab, noff);
+    const size_t total = packed_bytes(count, msg_len);
     cuspx_batch *b;
     int rc = oneshot_batch(ctx, CUSPX_OP_SIGN, set, count, total, &b);
     if (rc) return rc;
-    if ((rc = cuspx_batch_upload(b, count, sks, count, nullptr, slab.data(), total, noff.data(), msg_len, optrand,
-                                 nullptr)))
+    const SetParams &P = b->P;
+    const size_t sk_b = count * P.sk_bytes, opt_b = optrand ? count * P.n : 0, sig_b = count * P.sig_bytes;
+    Staging st;
+    if ((rc = oneshot_stage(ctx, al16(sk_b) + 2 * al16(count * 8) + al16(opt_b) + al16(total + 16) + al16(sig_b) +
+                                     al16(count * 4), st)))
+        return rc;
+    uint8_t *h_sk = (uint8_t *)st.take(sk_b);
+    uint64_t *h_off = (uint64_t *)st.take(count * 8);
+    uint64_t *h_len = (uint64_t *)st.take(count * 8);
+    uint8_t *h_opt = optrand ? (uint8_t *)st.take(opt_b) : nullptr;
+    uint8_t *h_msg = (uint8_t *)st.take(total + 16);
+    uint8_t *h_sig = (uint8_t *)st.take(sig_b);
+    int32_t *h_st = (int32_t *)st.take(count * 4);
+    memcpy(h_sk, sks, sk_b);
+    if (optrand) memcpy(h_opt, optrand, opt_b);
+    pack_staged(count, msgs, msg_off, msg_len, total, h_msg, h_off, h_len);
+    if ((rc = cuspx_batch_upload(b, count, h_sk, count, nullptr, h_msg, total, h_off, h_len, h_opt, nullptr)))
         return rc;
     if ((rc = cuspx_batch_run(b))) return rc;
-    std::vector<int32_t> st(count);
-    rc = cuspx_batch_download(b, sigs, nullptr, st.data());
-    if (status) memcpy(status, st.data(), count * 4);
-    return rc;
+    if ((rc = cuspx_batch_download(b, h_sig, nullptr, h_st))) return rc;
+    memcpy(sigs, h_sig, sig_b);
+    if (status) memcpy(status, h_st, count * 4);
+    return CUSPX_OK;
 }
 
 int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks, const uint8_t *msgs,
@@ -865,17 +935,33 @@ int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks
     if (count == 0) return CUSPX_OK;
     if (!pks || !msg_off || !msg_len || !sigs || !verdicts) return fail(ctx, CUSPX_EINVAL, "verify_batch: null buffer");
     std::lock_guard<std::mutex> lk(ctx->mu);
-    std::vector<uint8_t> slab;
-    std::vector<uint64_t> noff;
-    size_t total = pack_msgs(count, msgs, msg_off, msg_len, slab, noff);
+    const size_t total = packed_bytes(count, msg_len);
     cuspx_batch *b;
     int rc = oneshot_batch(ctx, CUSPX_OP_VERIFY, set, count, total, &b);
     if (rc) return rc;
-    if ((rc = cuspx_batch_upload(b, count, pks, count, nullptr, slab.data(), total, noff.data(), msg_len, sigs,
-                                 siglens)))
+    const SetParams &P = b->P;
+    const size_t pk_b = count * P.pk_bytes, sig_b = count * P.sig_bytes, sl_b = siglens ? count * 8 : 0;
+    Staging st;
+    if ((rc = oneshot_stage(ctx, al16(pk_b) + 2 * al16(count * 8) + al16(sl_b) + al16(sig_b) + al16(total + 16) +
+                                     al16(count * 4), st)))
+        return rc;
+    uint8_t *h_pk = (uint8_t *)st.take(pk_b);
+    uint64_t *h_off = (uint64_t *)st.take(count * 8);
+    uint64_t *h_len = (uint64_t *)st.take(count * 8);
+    uint64_t *h_sl = siglens ? (uint64_t *)st.take(sl_b) : nullptr;
+    uint8_t *h_sig = (uint8_t *)st.take(sig_b);
+    uint8_t *h_msg = (uint8_t *)st.take(total + 16);
+    int32_t *h_v = (int32_t *)st.take(count * 4);
+    memcpy(h_pk, pks, pk_b);
+    if (siglens) memcpy(h_sl, siglens, sl_b);
+    memcpy(h_sig, sigs, sig_b);
+    pack_staged(count, msgs, msg_off, msg_len, total, h_msg, h_off, h_len);
+    if ((rc = cuspx_batch_upload(b, count, h_pk, count, nullptr, h_msg, total, h_off, h_len, h_sig, h_sl)))
         return rc;
     if ((rc = cuspx_batch_run(b))) return rc;
-    return cuspx_batch_download(b, nullptr, nullptr, verdicts);
+    if ((rc = cuspx_batch_download(b, nullptr, nullptr, h_v))) return rc;
+    memcpy(verdicts, h_v, count * 4);
+    return CUSPX_OK;
 }
 
 // ---------------------------------------------------------------------------

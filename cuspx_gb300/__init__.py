@@ -386,11 +386,19 @@ class ServeCounters(ctypes.Structure):
         return out
 
 
+class LoadgenSample(ctypes.Structure):
+    _fields_ = [("set", ctypes.c_int32), ("key_id", ctypes.c_uint32), ("status", ctypes.c_int32),
+                ("pad", ctypes.c_uint32), ("mlen", ctypes.c_uint64), ("msg_off", ctypes.c_uint64),
+                ("sig_off", ctypes.c_uint64)]
+
+
 class LoadgenConfig(ctypes.Structure):
     _fields_ = [("rate", ctypes.c_double), ("seconds", ctypes.c_double), ("verify_frac", ctypes.c_double),
                 ("nsets", ctypes.c_int), ("sets", ctypes.POINTER(ctypes.c_int)), ("keys_per_set", ctypes.c_uint32),
                 ("min_len", ctypes.c_uint64), ("max_len", ctypes.c_uint64), ("corrupt_frac", ctypes.c_double),
-                ("seed", ctypes.c_uint64), ("pool", ctypes.c_int)]
+                ("seed", ctypes.c_uint64), ("pool", ctypes.c_int), ("sample_every", ctypes.c_uint32),
+                ("sample_max", ctypes.c_uint32), ("samples", ctypes.POINTER(LoadgenSample)),
+                ("arena", ctypes.c_void_p), ("arena_bytes", ctypes.c_size_t)]
 
 
 class LoadgenResult(ctypes.Structure):
@@ -401,7 +409,9 @@ class LoadgenResult(ctypes.Structure):
                                                  "mean_batch")] + \
                [(f, ctypes.c_double * 3) for f in ("sign_p50_bucket_us", "sign_p99_bucket_us",
                                                      "verify_p50_bucket_us", "verify_p99_bucket_us")] + \
-               [("launch_ms_mean", ctypes.c_double), ("launch_ms_max", ctypes.c_double)]
+               [("launch_ms_mean", ctypes.c_double), ("launch_ms_max", ctypes.c_double)] + \
+               [("set_sign_done", ctypes.c_uint64 * 8), ("set_verify_done", ctypes.c_uint64 * 8),
+                ("set_msg_units", ctypes.c_double * 8), ("sampled", ctypes.c_uint64)]
 
     def as_dict(self):
         return {f: (list(getattr(self, f)) if isinstance(getattr(self, f), ctypes.Array) else getattr(self, f))
@@ -506,14 +516,28 @@ class Server:
         self.L.cuspx_serve_reset_stats(self.h)
 
     def loadgen(self, rate, seconds, sets, keys_per_set, verify_frac=0.7, min_len=16, max_len=1 << 20,
-                corrupt_frac=0.0, seed=1, pool=64):
+                corrupt_frac=0.0, seed=1, pool=64, sample_every=0, sample_max=0, arena_bytes=0):
+        """Open-loop Poisson stream.  With sample_every > 0, one timed sign
+        request in sample_every keeps its signature (up to sample_max, within
+        arena_bytes); out["samples"] lists (set, key_id, status, msg, sig)."""
         arr = (ctypes.c_int * len(sets))(*sets)
+        smp = (LoadgenSample * max(1, sample_max))()
+        arena = ctypes.create_string_buffer(max(1, arena_bytes))
         cfg = LoadgenConfig(rate, seconds, verify_frac, len(sets), arr, keys_per_set, min_len, max_len,
-                            corrupt_frac, seed, pool)
+                            corrupt_frac, seed, pool, sample_every, sample_max,
+                            ctypes.cast(smp, ctypes.POINTER(LoadgenSample)), ctypes.cast(arena, ctypes.c_void_p),
+                            arena_bytes)
         res = LoadgenResult()
         rc = self.L.cuspx_serve_loadgen(self.h, ctypes.byref(cfg), ctypes.byref(res))
         out = res.as_dict()
         out["rc"] = rc
+        raw = arena.raw
+        out["samples"] = []
+        for i in range(res.sampled):
+            e = smp[i]
+            sigb = set_sizes(e.set)["sig"]
+            out["samples"].append((e.set, e.key_id, e.status, raw[e.msg_off:e.msg_off + e.mlen],
+                                   raw[e.sig_off:e.sig_off + sigb]))
         return out
 
 

@@ -898,8 +898,9 @@ int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, 
     if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
     if (count == 0) return CUSPX_OK;
     if (!sks || !msg_off || !msg_len || !sigs) return fail(ctx, CUSPX_EINVAL, "sign_batch: null buffer");
-    std::lock_guard<std::mutex> lk(ctx->mu);
     const size_t total = packed_bytes(count, msg_len);
+    if (!msgs && total) return fail(ctx, CUSPX_EINVAL, "sign_batch: msgs is null but a message is not empty");
+    std::lock_guard<std::mutex> lk(ctx->mu);
     cuspx_batch *b;
     int rc = oneshot_batch(ctx, CUSPX_OP_SIGN, set, count, total, &b);
     if (rc) return rc;
@@ -934,8 +935,9 @@ int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks
     if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
     if (count == 0) return CUSPX_OK;
     if (!pks || !msg_off || !msg_len || !sigs || !verdicts) return fail(ctx, CUSPX_EINVAL, "verify_batch: null buffer");
-    std::lock_guard<std::mutex> lk(ctx->mu);
     const size_t total = packed_bytes(count, msg_len);
+    if (!msgs && total) return fail(ctx, CUSPX_EINVAL, "verify_batch: msgs is null but a message is not empty");
+    std::lock_guard<std::mutex> lk(ctx->mu);
     cuspx_batch *b;
     int rc = oneshot_batch(ctx, CUSPX_OP_VERIFY, set, count, total, &b);
     if (rc) return rc;

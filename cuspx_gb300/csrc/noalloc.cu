@@ -66,7 +66,15 @@ extern "C" int cuspx_sign_noalloc(int set, size_t count, const uint8_t *d_sks, c
                                   uint8_t *d_sigs, int32_t *d_status, void *stream) {
     if (set < 0 || set >= kNumSets) return CUSPX_EINVAL;
     if (count == 0) return CUSPX_OK;
-    if (!d_sks || !d_msg_off || !d_msg_len || !d_sigs || !d_status) return CUSPX_EINVAL;
+    if (!d_sks || !d_msgs || !d_msg_off || !d_msg_len || !d_sigs || !d_status) return CUSPX_EINVAL;
+    // The kernels move keys, optrand, signatures, offsets and lengths as
+    // 8-byte words and read messages as 16-byte vectors; a misaligned
+    // pointer would fault on the device (and leave the context unusable),
+    // so it is refused here before anything is launched.
+    auto misaligned = [](const void *p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) != 0; };
+    if (misaligned(d_sks, 8) || misaligned(d_sigs, 8) || misaligned(d_optrand, 8) || misaligned(d_msg_off, 8) ||
+        misaligned(d_msg_len, 8) || misaligned(d_msgs, 16) || misaligned(d_status, 4))
+        return CUSPX_EINVAL;
     const SetDesc &sd = kSets[set];
     const SetParams P = make_params(sd);
     if (count > (1u << 20) || scratch_bytes(P, count) > CUSPX_NOALLOC_SCRATCH_BYTES) return CUSPX_ETOOBIG;

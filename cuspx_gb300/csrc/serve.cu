@@ -3,13 +3,13 @@
 // memory-budgeted admission, per-request latency, and an open-loop Poisson
 // load generator.
 //
-// Threads: callers submit and wait under one mutex; two scheduler threads,
+// Threads: callers submit and wait under one mutex; three scheduler threads,
 // one per message-length class, own every CUDA call on the serving batches
-// of their groups (pack into pinned staging, upload, graph launch,
-// asynchronous download, completion by event query), so a batch object is
-// only ever touched by one thread.  Packing a long-message launch copies up
-// to 64 MiB into pinned staging; with one scheduler, short launches and
-// completions waited behind that host work.
+// of their groups (pack into pinned staging, upload, launch, asynchronous
+// download, completion by event query), so a batch object is only ever
+// touched by one thread.  Packing a long-message launch copies up to 64 MiB
+// into pinned staging; with one scheduler, short launches and completions
+// waited behind that host work.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -54,7 +54,9 @@ struct Req {
     int32_t status = 0;
     int32_t expect = 1;     // load generator: expected verdict (1 = none)
     bool done = false;
+    bool waiting = false;   // a thread is in cuspx_serve_wait on this request
     unsigned flags = 0;
+    size_t admit_bytes = 0; // device bytes counted against the budget at submit
     Clock::time_point t0, t1;
 };
 
@@ -79,29 +81,76 @@ struct Slot {
     std::vector<Req *> reqs;
 };
 
-// Requests are grouped per (operation, set, length class): messages longer
-// than kLongMsg take milliseconds of serial hashing on one thread, so they
-// are launched in batches of their own that run beside the short ones
-// instead of holding every short request of a shared batch back.
-constexpr size_t kLongMsg = 16384;
-// Message area of one launch: a full batch of short messages, or 64 MiB of
-// long ones.  Slots are created once at this size and never re-created
-// (freeing device or pinned memory waits for the whole device).
+// Requests are grouped per (operation, set, length class).  Message hashing
+// is serial over the message on one thread (or one two-warp pair), and a
+// launch ends with its longest message, so requests are launched with others
+// of similar length: up to 16 KiB (<= 0.3 ms of hashing), up to 128 KiB
+// (<= 4 ms) and longer (up to ~33 ms per 1 MiB sign).  A 64 KiB request thus
+// never waits for a 1 MiB one in its own launch.
+constexpr int kClasses = 3;
+constexpr size_t kShortMsg = 16384;
+constexpr size_t kMidMsg = 131072;
+// Message area of one launch: a full batch of short messages, 32 MiB of
+// middle-class or 64 MiB of long messages.  Slots are created once at this
+// size and never re-created (freeing device or pinned memory waits for the
+// whole device).
+constexpr size_t kMidLaunchBytes = (size_t)32 << 20;
 constexpr size_t kLongLaunchBytes = (size_t)64 << 20;
+// a long-class launch holds at most 64 MiB / 128 KiB messages
+constexpr size_t kLongItems = kLongLaunchBytes / kMidMsg;
+
+int class_of(size_t mlen) { return mlen <= kShortMsg ? 0 : (mlen <= kMidMsg ? 1 : 2); }
 
 struct Group {
-    int op = 0, set = 0, long_class = 0;
+    int op = 0, set = 0, cls = 0;
     std::deque<Req *> pending;
     std::vector<Slot *> slots;
     size_t per_item = 0;
     SetParams P{};
 };
 
-double percentile(std::vector<float> v, double q) {
-    if (v.empty()) return 0.0;
-    size_t k = (size_t)std::min<double>(v.size() - 1, std::floor(q * (v.size() - 1) + 0.5));
-    std::nth_element(v.begin(), v.begin() + k, v.end());
-    return v[k];
+// Latency histogram: bin i holds [2^(i/64), 2^((i+1)/64)) microseconds
+// (1.1% wide), from 1 us to 2^31 us; a percentile is read as the
+// geometric middle of its bin.  Fixed memory, O(bins) per read.
+struct LatHist {
+    static constexpr int kPerOctave = 64, kBins = 64 * 31;
+    std::vector<uint64_t> bins = std::vector<uint64_t>(kBins, 0);
+    uint64_t n = 0;
+    void add(double us) {
+        int i = us <= 1.0 ? 0 : (int)std::floor(std::log2(us) * kPerOctave);
+        bins[std::min(std::max(i, 0), kBins - 1)]++;
+        n++;
+    }
+    // value of the sample of rank round(q (n - 1)) in sorted order
+    double pct(double q) const {
+        if (!n) return 0.0;
+        const uint64_t k = (uint64_t)std::min<double>((double)(n - 1), std::floor(q * (double)(n - 1) + 0.5));
+        uint64_t cum = 0;
+        for (int i = 0; i < kBins; i++) {
+            cum += bins[i];
+            if (cum > k) return std::exp2((i + 0.5) / kPerOctave);
+        }
+        return std::exp2((double)kBins / kPerOctave);
+    }
+    void clear() {
+        std::fill(bins.begin(), bins.end(), 0);
+        n = 0;
+    }
+};
+
+// Hash units of a request's message hashing (SHA-256 compressions or
+// Keccak-f[1600] permutations): H_msg for verify, PRF_msg and H_msg for
+// sign (hash_sha256.cu:99-145, :200-262; hash_shake256.cu:64-77, :96-130).
+double msg_units(int op, const SetDesc &sd, const SetParams &P, uint64_t mlen) {
+    const uint64_t n = sd.n;
+    if (sd.hash == 0) {
+        // SHA256(R || PK || m), then MGF1 blocks of 32 digest bytes
+        const uint64_t h = (3 * n + mlen + 9 + 63) / 64 + (P.dgst_bytes + 31) / 32;
+        // HMAC: ipad block, optrand || m, then opad block and the inner digest
+        return (double)(op == CUSPX_OP_VERIFY ? h : h + 3 + (n + mlen + 9 + 63) / 64);
+    }
+    const uint64_t h = (3 * n + mlen) / 136 + 1;
+    return (double)(op == CUSPX_OP_VERIFY ? h : h + (2 * n + mlen) / 136 + 1);
 }
 
 }  // namespace
@@ -111,20 +160,23 @@ struct cuspx_server {
     cuspx_serve_config cfg{};
     int device = 0;
     std::mutex mu;
-    std::condition_variable cv_sched[2], cv_done;   // cv_sched[length class]
-    std::thread th[2];
+    std::condition_variable cv_sched[kClasses], cv_done;   // cv_sched[length class]
+    std::thread th[kClasses];
     bool stop = false;
     std::vector<KeyTable> keys;
-    std::vector<Group> groups;   // index ((op - 1) * kNumSets + set) * 2 + long_class
+    std::vector<Group> groups;   // index ((op - 1) * kNumSets + set) * kClasses + class
     std::unordered_map<uint64_t, Req *> live;
     uint64_t next_ticket = 1;
-    size_t pending_total = 0, bytes_inflight = 0, bytes_peak = 0, bytes_alloc = 0;
+    size_t pending_total = 0, pending_bytes = 0, bytes_inflight = 0, bytes_peak = 0;
     uint64_t submitted = 0, completed = 0, refused = 0, failed = 0, launches = 0, batched = 0;
     uint64_t sign_done = 0, verify_done = 0, wrong = 0;
     double launch_ms_sum = 0, launch_ms_max = 0;
-    std::vector<float> lat_sign, lat_verify;
-    std::vector<float> lat_bucket[2][3];   // [sign, verify][<= 1 KiB, <= 64 KiB, > 64 KiB]
+    LatHist lat_sign, lat_verify;
+    LatHist lat_bucket[2][3];   // [sign, verify][<= 1 KiB, <= 64 KiB, > 64 KiB]
+    uint64_t done_by_set[2][kNumSets] = {};   // [sign, verify][set]
+    double msg_units_by_set[kNumSets] = {};
     Clock::time_point last_done;
+    Group &group(int op, int set, int cls) { return groups[((op - 1) * kNumSets + set) * kClasses + cls]; }
 };
 
 static int len_bucket(size_t mlen) { return mlen <= 1024 ? 0 : (mlen <= 65536 ? 1 : 2); }
@@ -156,22 +208,27 @@ static void free_slot(Slot *sl) {
 }
 
 static size_t class_msg_bytes(const cuspx_server *s, const Group &g) {
-    return g.long_class ? kLongLaunchBytes : (size_t)s->cfg.max_batch * (kLongMsg + 16);
+    return g.cls == 2 ? kLongLaunchBytes
+                      : (g.cls == 1 ? kMidLaunchBytes : (size_t)s->cfg.max_batch * (kShortMsg + 16));
+}
+static size_t class_items(const cuspx_server *s, const Group &g) {
+    return g.cls == 2 ? std::min<size_t>(s->cfg.max_batch, kLongItems) : (size_t)s->cfg.max_batch;
 }
 
 // Create a slot's batch and pinned staging once, at the full size of its
-// group (max_batch items, the class's message area).
+// group (the class's items and message area).
 static bool size_slot(cuspx_server *s, Group &g, Slot *sl) {
     const SetParams &P = g.P;
     if (sl->b) return true;
-    const size_t cap = (size_t)s->cfg.max_batch;
+    const size_t cap = class_items(s, g);
     const size_t msg_cap = class_msg_bytes(s, g);
     if (cuspx_batch_create(s->ctx, g.op, g.set, cap, msg_cap, 1, &sl->b) != CUSPX_OK) return false;
     batch_direct_launch(sl->b, true);   // no graph instantiation while serving
-    // short-message launches run ahead of long-message ones on the GPU
+    // short-message launches run ahead of middle ones, those ahead of long
+    // ones on the GPU (lo is the least urgent priority, hi the most)
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    batch_set_stream_priority(sl->b, g.long_class ? lo : hi);
+    batch_set_stream_priority(sl->b, g.cls == 0 ? hi : (g.cls == 1 ? (lo + hi) / 2 : lo));
     const KeyTable &kt = s->keys[g.set];
     cuspx_batch_bind_keys(sl->b, g.op == CUSPX_OP_SIGN ? kt.d_sk : kt.d_pk, kt.cap);
     auto host = [](void **p, size_t bytes) { return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };
@@ -241,15 +298,20 @@ static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
             r->out.assign(sl->h_out + i * P.sig_bytes, sl->h_out + (i + 1) * P.sig_bytes);
         r->t1 = now;
         r->done = true;
-        const float us = std::chrono::duration<float, std::micro>(now - r->t0).count();
-        if (g.op == CUSPX_OP_SIGN) {
-            s->lat_sign.push_back(us);
+        const double us = std::chrono::duration<double, std::micro>(now - r->t0).count();
+        const int o = g.op == CUSPX_OP_SIGN ? 0 : 1;
+        if (o == 0) {
+            s->lat_sign.add(us);
             s->sign_done++;
         } else {
-            s->lat_verify.push_back(us);
+            s->lat_verify.add(us);
             s->verify_done++;
         }
-        s->lat_bucket[g.op == CUSPX_OP_SIGN ? 0 : 1][len_bucket(r->mlen)].push_back(us);
+        s->lat_bucket[o][len_bucket(r->mlen)].add(us);
+        if (ok) {
+            s->done_by_set[o][g.set]++;
+            s->msg_units_by_set[g.set] += msg_units(g.op, kSets[g.set], P, r->mlen);
+        }
         if (r->expect != 1 && r->status != r->expect) s->wrong++;
         s->completed++;
         if (r->flags & CUSPX_SUBMIT_DETACH) {
@@ -276,7 +338,7 @@ static void scheduler(cuspx_server *s, int lc) {
         bool any_busy = false;
         size_t class_pending = 0;
         for (Group &g : s->groups) {
-            if (g.long_class != lc) continue;
+            if (g.cls != lc) continue;
             class_pending += g.pending.size();
             for (Slot *sl : g.slots) {
                 if (!sl->busy) continue;
@@ -297,7 +359,7 @@ static void scheduler(cuspx_server *s, int lc) {
         const auto now = Clock::now();
         Clock::time_point next_wake = now + std::chrono::microseconds(50);
         for (Group &g : s->groups) {
-            if (g.long_class != lc) continue;
+            if (g.cls != lc) continue;
             while (!g.pending.empty()) {
                 int inflight = 0;
                 Slot *free_sl = nullptr;
@@ -305,7 +367,8 @@ static void scheduler(cuspx_server *s, int lc) {
                     if (sl->busy) inflight++;
                     else if (!free_sl) free_sl = sl;
                 }
-                const bool full = g.pending.size() >= (size_t)s->cfg.max_batch;
+                const size_t items = class_items(s, g);
+                const bool full = g.pending.size() >= items;
                 const bool waited = now - g.pending.front()->t0 >= window;
                 if (!(full || waited || inflight == 0)) {
                     next_wake = std::min(next_wake, g.pending.front()->t0 + window);
@@ -316,27 +379,26 @@ static void scheduler(cuspx_server *s, int lc) {
                     free_sl = new Slot();
                     g.slots.push_back(free_sl);
                 }
-                // take as many as fit the batch size, the launch's message
-                // area and the memory budget
+                // take as many as fit the launch's items and message area
+                // (their device bytes were admitted against the budget when
+                // they were submitted, so pending + in-flight stays within it)
                 size_t n = 0, bytes = 0, mbytes = 0;
                 const size_t mcap = class_msg_bytes(s, g);
                 for (Req *r : g.pending) {
-                    if (n == (size_t)s->cfg.max_batch) break;
+                    if (n == items) break;
                     const size_t m16 = (r->mlen + 15) & ~(size_t)15;
                     if (mbytes + m16 > mcap) break;
                     mbytes += m16;
-                    const size_t add = g.per_item + m16;
-                    if (s->bytes_inflight + bytes + add > s->cfg.mem_budget && n > 0) break;
-                    if (s->bytes_inflight + bytes + add > s->cfg.mem_budget && s->bytes_inflight > 0) break;
-                    bytes += add;
+                    bytes += r->admit_bytes;
                     n++;
                 }
-                if (n == 0) break;   // budget full: wait for completions
+                if (n == 0) break;
                 for (size_t i = 0; i < n; i++) {
                     free_sl->reqs.push_back(g.pending.front());
                     g.pending.pop_front();
                 }
                 s->pending_total -= n;
+                s->pending_bytes -= bytes;
                 free_sl->busy = true;
                 free_sl->bytes = bytes;
                 s->bytes_inflight += bytes;
@@ -371,19 +433,18 @@ int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_serv
     if (!s->cfg.max_queue) s->cfg.max_queue = 1u << 20;
     cudaGetDevice(&s->device);
     s->keys.resize(kNumSets);
-    s->groups.resize(4 * kNumSets);
+    s->groups.resize(2 * kNumSets * kClasses);
     for (int op = 1; op <= 2; op++)
         for (int set = 0; set < kNumSets; set++)
-            for (int lc = 0; lc < 2; lc++) {
-                Group &g = s->groups[((op - 1) * kNumSets + set) * 2 + lc];
+            for (int lc = 0; lc < kClasses; lc++) {
+                Group &g = s->group(op, set, lc);
                 g.op = op;
                 g.set = set;
-                g.long_class = lc;
+                g.cls = lc;
                 g.P = make_params(kSets[set]);
                 g.per_item = item_bytes(op, g.P);
             }
-    s->th[0] = std::thread(scheduler, s, 0);
-    s->th[1] = std::thread(scheduler, s, 1);
+    for (int lc = 0; lc < kClasses; lc++) s->th[lc] = std::thread(scheduler, s, lc);
     *out = s;
     return CUSPX_OK;
 }
@@ -394,8 +455,8 @@ void cuspx_serve_destroy(cuspx_server *s) {
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
     }
-    for (int lc = 0; lc < 2; lc++) s->cv_sched[lc].notify_all();
-    for (int lc = 0; lc < 2; lc++)
+    for (int lc = 0; lc < kClasses; lc++) s->cv_sched[lc].notify_all();
+    for (int lc = 0; lc < kClasses; lc++)
         if (s->th[lc].joinable()) s->th[lc].join();
     for (Group &g : s->groups) {
         for (Slot *sl : g.slots) {
@@ -449,7 +510,7 @@ static int add_rows(cuspx_server *s, int set, size_t count, const uint8_t *rows,
     return CUSPX_OK;
 }
 
-// Create every launch slot of (op, set) -- both length classes, max_inflight
+// Create every launch slot of (op, set) -- all length classes, max_inflight
 // each -- now instead of on first use: a slot's device batch and pinned
 // staging (64 MiB for long messages) take milliseconds to allocate, and
 // device allocation can wait for work already on the GPU, so creating them
@@ -459,8 +520,8 @@ int cuspx_serve_prepare(cuspx_server *s, int op, int set) {
     if (cudaSetDevice(s->device) != cudaSuccess) return CUSPX_ECUDA;
     std::lock_guard<std::mutex> lk(s->mu);
     if (int rc = ensure_table(s, set)) return rc;
-    for (int lc = 0; lc < 2; lc++) {
-        Group &g = s->groups[((op - 1) * kNumSets + set) * 2 + lc];
+    for (int lc = 0; lc < kClasses; lc++) {
+        Group &g = s->group(op, set, lc);
         while ((int)g.slots.size() < s->cfg.max_inflight) {
             Slot *sl = new Slot();
             if (!size_slot(s, g, sl)) {
@@ -507,13 +568,17 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     r->siglen = op == CUSPX_OP_VERIFY ? siglen : 0;
     std::unique_lock<std::mutex> lk(s->mu);
     const KeyTable &kt = s->keys[set];
-    Group &g = s->groups[((op - 1) * kNumSets + set) * 2 + (mlen > kLongMsg ? 1 : 0)];
+    Group &g = s->group(op, set, class_of(mlen));
+    r->admit_bytes = g.per_item + ((mlen + 15) & ~(size_t)15);
     int rc = CUSPX_OK;
     if (s->stop) rc = CUSPX_EBUSY;
     else if (key_id >= kt.n || (op == CUSPX_OP_SIGN && !kt.has_sk[key_id])) rc = CUSPX_EINVAL;
-    else if (g.per_item + mlen > s->cfg.mem_budget) rc = CUSPX_ENOMEM;
+    else if (r->admit_bytes > s->cfg.mem_budget) rc = CUSPX_ENOMEM;   // could never be admitted
     else if (mlen + 16 > kLongLaunchBytes) rc = CUSPX_ETOOBIG;
     else if (s->pending_total >= s->cfg.max_queue) rc = CUSPX_EBUSY;
+    // admission by device-memory budget: the bytes of everything pending or
+    // in flight, this request included
+    else if (s->pending_bytes + s->bytes_inflight + r->admit_bytes > s->cfg.mem_budget) rc = CUSPX_EBUSY;
     if (rc != CUSPX_OK) {
         s->refused++;
         lk.unlock();
@@ -525,11 +590,12 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     s->live[r->ticket] = r;
     g.pending.push_back(r);
     s->pending_total++;
+    s->pending_bytes += r->admit_bytes;
     s->submitted++;
     if (ticket) *ticket = r->ticket;
-    const bool kick = g.pending.size() == 1 || g.pending.size() >= (size_t)s->cfg.max_batch;
+    const bool kick = g.pending.size() == 1 || g.pending.size() >= class_items(s, g);
     lk.unlock();
-    if (kick) s->cv_sched[g.long_class].notify_one();
+    if (kick) s->cv_sched[g.cls].notify_one();
     return CUSPX_OK;
 }
 
@@ -545,24 +611,28 @@ int cuspx_serve_wait(cuspx_server *s, uint64_t ticket, long timeout_us, uint8_t 
     auto it = s->live.find(ticket);
     if (it == s->live.end()) return CUSPX_EINVAL;
     Req *r = it->second;
+    // a detached request is freed by its completion, and a request has one
+    // waiter: a second one would wake to a freed request
+    if ((r->flags & CUSPX_SUBMIT_DETACH) || r->waiting) return CUSPX_EINVAL;
+    r->waiting = true;
     auto pred = [&] { return r->done; };
     if (timeout_us < 0) s->cv_done.wait(lk, pred);
-    else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), pred)) return CUSPX_ETIMEDOUT;
+    else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), pred)) {
+        r->waiting = false;
+        return CUSPX_ETIMEDOUT;
+    }
     if (sig_out && !r->out.empty()) memcpy(sig_out, r->out.data(), r->out.size());
     if (status) *status = r->status;
     if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(r->t1 - r->t0).count();
-    s->live.erase(it);
+    s->live.erase(r->ticket);
     delete r;
     return CUSPX_OK;
 }
 
 int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st) {
     if (!s || !st) return CUSPX_EINVAL;
-    std::vector<float> ls, lv, lb[2][3];
+    std::lock_guard<std::mutex> lk(s->mu);
     {
-        std::lock_guard<std::mutex> lk(s->mu);
-        for (int o = 0; o < 2; o++)
-            for (int b = 0; b < 3; b++) lb[o][b] = s->lat_bucket[o][b];
         st->submitted = s->submitted;
         st->completed = s->completed;
         st->refused = s->refused;
@@ -575,20 +645,18 @@ int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st) {
         st->mean_batch = s->launches ? (double)s->batched / s->launches : 0.0;
         st->launch_ms_mean = s->launches ? s->launch_ms_sum / s->launches : 0.0;
         st->launch_ms_max = s->launch_ms_max;
-        ls = s->lat_sign;
-        lv = s->lat_verify;
     }
-    st->sign_p50_us = percentile(ls, 0.50);
-    st->sign_p99_us = percentile(ls, 0.99);
-    st->verify_p50_us = percentile(lv, 0.50);
-    st->verify_p99_us = percentile(lv, 0.99);
+    st->sign_p50_us = s->lat_sign.pct(0.50);
+    st->sign_p99_us = s->lat_sign.pct(0.99);
+    st->verify_p50_us = s->lat_verify.pct(0.50);
+    st->verify_p99_us = s->lat_verify.pct(0.99);
     for (int b = 0; b < 3; b++) {
-        st->sign_p50_bucket_us[b] = percentile(lb[0][b], 0.50);
-        st->sign_p99_bucket_us[b] = percentile(lb[0][b], 0.99);
-        st->verify_p50_bucket_us[b] = percentile(lb[1][b], 0.50);
-        st->verify_p99_bucket_us[b] = percentile(lb[1][b], 0.99);
-        st->bucket_count[0][b] = lb[0][b].size();
-        st->bucket_count[1][b] = lb[1][b].size();
+        st->sign_p50_bucket_us[b] = s->lat_bucket[0][b].pct(0.50);
+        st->sign_p99_bucket_us[b] = s->lat_bucket[0][b].pct(0.99);
+        st->verify_p50_bucket_us[b] = s->lat_bucket[1][b].pct(0.50);
+        st->verify_p99_bucket_us[b] = s->lat_bucket[1][b].pct(0.99);
+        st->bucket_count[0][b] = s->lat_bucket[0][b].n;
+        st->bucket_count[1][b] = s->lat_bucket[1][b].n;
     }
     return CUSPX_OK;
 }
@@ -604,6 +672,8 @@ int cuspx_serve_reset_stats(cuspx_server *s) {
     s->lat_verify.clear();
     for (auto &o : s->lat_bucket)
         for (auto &b : o) b.clear();
+    memset(s->done_by_set, 0, sizeof(s->done_by_set));
+    memset(s->msg_units_by_set, 0, sizeof(s->msg_units_by_set));
     return CUSPX_OK;
 }
 
@@ -642,6 +712,16 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
         cuspx_set_sizes(set, nullptr, nullptr, &sigb, nullptr, nullptr);
         std::vector<uint64_t> tickets(pool);
         pools[si].resize(pool);
+        int waited = 0;   // entries [0, waited) have their signatures
+        auto wait_upto = [&](int upto) -> int {
+            for (; waited < upto; waited++) {
+                Entry &e = pools[si][waited];
+                int32_t st = 0;
+                int rc = cuspx_serve_wait(s, tickets[waited], 120000000L, e.sig.data(), &st, nullptr);
+                if (rc || st) return rc ? rc : CUSPX_ECUDA;
+            }
+            return CUSPX_OK;
+        };
         for (int i = 0; i < pool; i++) {
             Entry &e = pools[si][i];
             e.mlen = draw_len();
@@ -649,13 +729,15 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
             e.key = (uint32_t)(rng() % c->keys_per_set);
             e.sig.resize(sigb);
             int rc = submit(s, CUSPX_OP_SIGN, set, e.key, e.m, e.mlen, nullptr, 0, CUSPX_SUBMIT_BORROW, 1, &tickets[i]);
+            if (rc == CUSPX_EBUSY) {   // over the admission budget: let the earlier ones finish
+                if ((rc = wait_upto(i))) return rc;
+                rc = submit(s, CUSPX_OP_SIGN, set, e.key, e.m, e.mlen, nullptr, 0, CUSPX_SUBMIT_BORROW, 1, &tickets[i]);
+            }
             if (rc) return rc;
         }
+        if (int rc = wait_upto(pool)) return rc;
         for (int i = 0; i < pool; i++) {
             Entry &e = pools[si][i];
-            int32_t st = 0;
-            int rc = cuspx_serve_wait(s, tickets[i], 120000000L, e.sig.data(), &st, nullptr);
-            if (rc || st) return rc ? rc : CUSPX_ECUDA;
             e.bad = e.sig;
             const size_t pos = (size_t)(rng() % sigb);
             e.bad[pos] ^= (uint8_t)(1u << (rng() % 8));
@@ -666,6 +748,17 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
     std::exponential_distribution<double> gap(c->rate);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     uint64_t offered = 0, refused = 0;
+    // sampled sign requests: kept (not detached) and copied out after the run
+    struct Pick {
+        uint64_t ticket;
+        int set;
+        uint32_t key;
+        const uint8_t *m;
+        size_t mlen, sigb;
+    };
+    std::vector<Pick> picks;
+    uint64_t signs_offered = 0;
+    size_t arena_used = 0;
     const auto t0 = Clock::now();
     double t_next = 0.0;
     while (true) {
@@ -690,8 +783,20 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
                         CUSPX_SUBMIT_BORROW | CUSPX_SUBMIT_DETACH, corrupt ? -1 : 0, nullptr);
         } else {
             const size_t L = draw_len();
-            rc = submit(s, CUSPX_OP_SIGN, set, (uint32_t)(rng() % c->keys_per_set), buf.data() + draw_off(L), L,
-                        nullptr, 0, CUSPX_SUBMIT_BORROW | CUSPX_SUBMIT_DETACH, 1, nullptr);
+            const uint32_t key = (uint32_t)(rng() % c->keys_per_set);
+            const uint8_t *m = buf.data() + draw_off(L);
+            size_t sigb = 0;
+            cuspx_set_sizes(set, nullptr, nullptr, &sigb, nullptr, nullptr);
+            const bool pick = c->sample_every && c->samples && c->arena && signs_offered % c->sample_every == 0 &&
+                              picks.size() < c->sample_max && arena_used + L + sigb <= c->arena_bytes;
+            signs_offered++;
+            uint64_t t = 0;
+            rc = submit(s, CUSPX_OP_SIGN, set, key, m, L, nullptr, 0,
+                        CUSPX_SUBMIT_BORROW | (pick ? 0u : CUSPX_SUBMIT_DETACH), 1, &t);
+            if (pick && rc == CUSPX_OK) {
+                picks.push_back(Pick{t, set, key, m, L, sigb});
+                arena_used += L + sigb;
+            }
         }
         if (rc) refused++;
     }
@@ -709,6 +814,31 @@ int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *c, cuspx_lo
         std::lock_guard<std::mutex> lk(s->mu);
         wall = std::chrono::duration<double>(s->last_done - t0).count();
         wrong = s->wrong;
+        for (int si = 0; si < 8; si++) {
+            const bool in = si < c->nsets;
+            out->set_sign_done[si] = in ? s->done_by_set[0][c->sets[si]] : 0;
+            out->set_verify_done[si] = in ? s->done_by_set[1][c->sets[si]] : 0;
+            out->set_msg_units[si] = in ? s->msg_units_by_set[c->sets[si]] : 0.0;
+        }
+    }
+    // the sampled signatures (every sampled request completed in the drain
+    // above, or its wait runs out here)
+    size_t at = 0;
+    out->sampled = 0;
+    for (const Pick &pk : picks) {
+        cuspx_loadgen_sample &smp = c->samples[out->sampled];
+        smp.set = pk.set;
+        smp.key_id = pk.key;
+        smp.mlen = pk.mlen;
+        smp.msg_off = at;
+        smp.sig_off = at + pk.mlen;
+        smp.pad = 0;
+        int32_t sst = -3;
+        if (cuspx_serve_wait(s, pk.ticket, 10000000L, c->arena + smp.sig_off, &sst, nullptr) != CUSPX_OK) continue;
+        if (pk.mlen) memcpy(c->arena + smp.msg_off, pk.m, pk.mlen);
+        smp.status = sst;
+        at += pk.mlen + pk.sigb;
+        out->sampled++;
     }
     out->offered = offered;
     out->completed = st.completed;

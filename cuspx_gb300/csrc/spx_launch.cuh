@@ -6,6 +6,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "spx_kernels.cuh"
 #include "spx_verify.cuh"
 
@@ -84,6 +86,22 @@ extern FamilyOps g_family[2][3][2];
 
 inline unsigned ceil_div(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// SM count of the current device, queried once per device (a launch-shape
+// input of the small-batch mappings; 1 if the query fails)
+inline int device_sms() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        v = sms > 0 ? sms : 1;
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
 // finish key generation: sk.ROOT = pk.ROOT = top root, pk.PUB_SEED = sk.PUB_SEED
 template <int n>
 __global__ void k_keygen_finish(KeygenArgs A) {
@@ -146,10 +164,8 @@ struct Family {
         if constexpr (kPersistVerify) {
             int wpb = tu.verify_block / 32;
             wpb = wpb < 1 ? 1 : (wpb > 4 ? 4 : wpb);
-            int dev = 0, sms = 0, occ = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (sms < 1) sms = 1;
+            const int sms = device_sms();
+            int occ = 0;
             // Items per warp: one item's serial critical path (~d x 20
             // compressions) sets the time of a small batch, and a warp
             // holding several items runs their paths at a fraction of its
@@ -222,9 +238,10 @@ struct Family {
         {
             const int b = tu.fors_block;
             // small batches: spread each tree over more lanes until the launch
-            // has about one full wave of threads (152 SMs x 128), for latency
+            // has about one full wave of threads (SMs x 128), for latency
+            const uint64_t wave = (uint64_t)device_sms() * 128;
             int g = tu.fors_lanes_log2 < P.a ? tu.fors_lanes_log2 : P.a;
-            while (g < 5 && g < P.a && (((uint64_t)A.count * P.k) << g) < 152ull * 128) g++;
+            while (g < 5 && g < P.a && (((uint64_t)A.count * P.k) << g) < wave) g++;
             const uint64_t threads = (((uint64_t)A.count * P.k) << g);
             k_fors_sign<HF><<<ceil_div(threads, b), b, (size_t)b * (P.a - g + 1) * W * 4, sf>>>(P, A, g);
             CUSPX_MARK(pt, "k_fors_sign", s);

@@ -164,8 +164,14 @@ int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *
  * a message slab with 16-byte aligned offsets, readable up to the next
  * multiple of 16 past each message; optrand count x n or NULL for the
  * reference's 0xAD bytes; count x sig_bytes signatures; count statuses) and
- * the cudaStream_t to run on (NULL: legacy default stream).  The call is
- * asynchronous on that stream and allocates nothing: its scratch is an
+ * the cudaStream_t to run on (NULL: legacy default stream).
+ *   - Alignment: d_msgs must be 16-byte aligned; d_sks, d_optrand, d_sigs,
+ *     d_msg_off and d_msg_len 8-byte aligned; d_status 4-byte aligned.
+ *     Otherwise CUSPX_EINVAL is returned and nothing is launched.  The
+ *     per-item offsets live on the device and cannot be checked: each must
+ *     be a multiple of 16.  d_msgs must not be NULL, even when every
+ *     message is empty (the lengths are not visible to the host).
+ * The call is asynchronous on that stream and allocates nothing: its scratch is an
  * 8 MiB array in the library's device image, held by every GPU that loads
  * the library until the process exits.
  *   - Limit: count must fit the 8 MiB scratch; the per-signature need is

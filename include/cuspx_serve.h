@@ -5,22 +5,30 @@
  * that allocate, launch and free per batch (sign.cu:5920-5963).  Here
  * requests are admitted as they arrive and continuously batched:
  *   - keys live on the device in a per-set resident table (sk and pk rows);
- *   - scheduler threads (one for messages up to 16 KiB, one for longer
- *     ones) group pending requests per (operation, set, length class) and
- *     launch a batch when the batch is full, the oldest request has waited
- *     `window_us`, or no launch of that group is in flight;
+ *   - requests are split into three message-length classes -- up to
+ *     16 KiB, up to 128 KiB, longer -- because message hashing is serial
+ *     over the message (a 1 MiB sign hashes for ~33 ms) and a launch ends
+ *     with its longest message; one scheduler thread per class groups
+ *     pending requests per (operation, set, class) and launches a batch when
+ *     the batch is full, the oldest request has waited `window_us`, or no
+ *     launch of that group is in flight;
  *   - up to `max_inflight` launches per group run at once on their own
- *     streams, so requests arriving while others are on the GPU are admitted
+ *     streams (short class at the highest stream priority, long class at the
+ *     lowest), so requests arriving while others are on the GPU are admitted
  *     as slots free up and overlap on the device;
- *   - a launch is admitted only while the device bytes of all in-flight
- *     launches stay within `mem_budget`; submissions beyond `max_queue`
- *     pending requests are refused with CUSPX_EBUSY;
- *   - requests with messages over 16 KiB are batched apart from shorter ones
- *     (their serial message hashing would hold a shared batch back); a
- *     launch carries at most 64 MiB of long messages, and a single message
- *     over 64 MiB is refused with CUSPX_ETOOBIG;
+ *   - admission by device-memory budget: every request counts the device
+ *     bytes its launch will need (scratch plus message) from submission on;
+ *     a submission that would take pending plus in-flight bytes over
+ *     `mem_budget` is refused with CUSPX_EBUSY, and so is one beyond
+ *     `max_queue` pending requests.  The budget thus bounds both the device
+ *     memory of in-flight launches and the work queued ahead of a request;
+ *   - a launch carries at most 32 MiB of middle-class or 64 MiB of
+ *     long-class messages; a single message over 64 MiB is refused with
+ *     CUSPX_ETOOBIG;
  *   - per-request latency (submit to result on the host) feeds p50/p99,
- *     overall and per message-length bucket.
+ *     overall and per message-length bucket, from fixed log-spaced
+ *     histograms (bins 1.1% wide), so memory stays bounded however long the
+ *     server runs.
  * Results of a request do not depend on what it was batched with.
  */
 #ifndef CUSPX_SERVE_H
@@ -38,7 +46,7 @@ extern "C" {
 typedef struct cuspx_server cuspx_server;
 
 typedef struct {
-    size_t mem_budget;   /* device bytes for in-flight launches (0: 8 GiB) */
+    size_t mem_budget;   /* device bytes of pending and in-flight requests (0: 8 GiB) */
     int max_batch;       /* requests per launch (0: 1024) */
     int max_inflight;    /* launches in flight per (operation, set) (0: 3) */
     int window_us;       /* batching window (0: 500 us) */
@@ -82,13 +90,24 @@ int cuspx_serve_submit(cuspx_server *s, int op, int set, uint32_t key_id, const 
 /* Wait up to timeout_us (< 0: forever) for a request.  On completion copies
  * the signature (sign) into sig_out if not NULL, the status (sign: 0 or
  * <0; verify: 0 accept / -1 reject) and latency, releases the ticket and
- * returns CUSPX_OK; otherwise returns CUSPX_ETIMEDOUT. */
+ * returns CUSPX_OK; otherwise returns CUSPX_ETIMEDOUT.  One thread waits on
+ * a ticket at a time: a second concurrent wait on it, or a wait on a
+ * released or detached ticket, returns CUSPX_EINVAL. */
 int cuspx_serve_wait(cuspx_server *s, uint64_t ticket, long timeout_us, uint8_t *sig_out, int32_t *status,
                      double *latency_us);
 int cuspx_serve_stats(cuspx_server *s, cuspx_serve_counters *st);
 int cuspx_serve_reset_stats(cuspx_server *s);
 
 /* ---- open-loop Poisson load generator ---------------------------------- */
+/* one sampled sign request of the load generator (see sample_every) */
+typedef struct cuspx_loadgen_sample {
+    int32_t set;
+    uint32_t key_id;
+    int32_t status;   /* the sign request's status */
+    uint32_t pad;
+    uint64_t mlen, msg_off, sig_off;
+} cuspx_loadgen_sample;
+
 typedef struct {
     double rate;            /* arrivals per second */
     double seconds;         /* length of the arrival window */
@@ -100,6 +119,18 @@ typedef struct {
     double corrupt_frac;    /* verify requests with one seeded byte flipped */
     uint64_t seed;
     int pool;               /* pre-signed (message, signature) pairs per set for verify */
+    /* Sampling of the timed sign requests, so that a caller can check the
+     * signatures the stream produced (e.g. against an independent
+     * implementation): one sign request in every `sample_every` (0: none)
+     * keeps its result, up to `sample_max` samples; sample i's message and
+     * signature are copied to arena + samples[i].msg_off / sig_off while
+     * arena_bytes last.  The sampled requests are otherwise submitted like
+     * the rest (same lengths, sets and timing). */
+    uint32_t sample_every;
+    uint32_t sample_max;
+    cuspx_loadgen_sample *samples;
+    uint8_t *arena;
+    size_t arena_bytes;
 } cuspx_loadgen_config;
 
 typedef struct {
@@ -109,6 +140,12 @@ typedef struct {
     double mean_batch;
     double sign_p50_bucket_us[3], sign_p99_bucket_us[3], verify_p50_bucket_us[3], verify_p99_bucket_us[3];
     double launch_ms_mean, launch_ms_max;
+    /* per entry of cfg->sets (the first 8): completed signs and verifies,
+     * and the hash units of their message hashing (SHA-256 compressions or
+     * Keccak-f[1600] permutations of PRF_msg and H_msg) */
+    uint64_t set_sign_done[8], set_verify_done[8];
+    double set_msg_units[8];
+    uint64_t sampled;       /* samples written */
 } cuspx_loadgen_result;
 
 int cuspx_serve_loadgen(cuspx_server *s, const cuspx_loadgen_config *cfg, cuspx_loadgen_result *out);

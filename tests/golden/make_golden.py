@@ -17,6 +17,13 @@ inputs and records what the reference produced:
 
 Run from the repository root (needs the reference tree and nvcc):
     python tests/golden/make_golden.py [set ...]
+
+With --release it writes tests/golden/<set>_release.json instead, from the
+reference built without DEBUG_MODE (oracle/build_ref.sh --release): the
+keypair seed and every optrand then come from the DRBG, so the record pins
+the DRBG consumption of crypto_sign_keypair (3n bytes), crypto_sign_signature
+and crypto_sign (n bytes each) in call order:
+    python tests/golden/make_golden.py --release [set ...]
 """
 import hashlib
 import json
@@ -47,11 +54,24 @@ def lengths_for(setname, n):
     return sorted(set(x for x in base + edges if x >= 0))
 
 
+RELEASE_SETS = ["sha256-128f", "shake256-256f", "sha256-192f"]
+
+
+def release_messages():
+    """Three fixed messages (0, 33 and 1000 bytes) that do not touch the DRBG."""
+    return [b"", hashlib.shake_256(b"release m1").digest(33), hashlib.shake_256(b"release m2").digest(1000)]
+
+
+RELEASE_ENTROPY = bytes((7 * i + 3) & 0xFF for i in range(48))
+
+
 class Ref:
-    def __init__(self, setname):
-        exe = os.path.join(ROOT, "oracle", "_ref", setname, "ref_golden")
+    def __init__(self, setname, release=False):
+        sub = setname + ("-release" if release else "")
+        exe = os.path.join(ROOT, "oracle", "_ref", sub, "ref_golden")
         if not os.path.exists(exe):
-            subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), setname], check=True)
+            cmd = [os.path.join(ROOT, "oracle", "build_ref.sh")] + (["--release"] if release else []) + [setname]
+            subprocess.run(cmd, check=True)
         self.p = subprocess.Popen([exe], stdin=subprocess.PIPE, stdout=subprocess.PIPE, text=True)
 
     def __call__(self, line):
@@ -125,6 +145,43 @@ def gen(setname):
     print(setname, len(cases), "cases")
 
 
+def gen_release(setname):
+    """The reference's release call sequence: keypair, sign, crypto_sign,
+    open, verify, a second keypair and sign, then 16 more DRBG bytes."""
+    ref = Ref(setname, release=True)
+    n, pkb, skb, sigb, seedb = map(int, ref("info").split())
+    m0, m1, m2 = release_messages()
+    ref("drbg_init " + RELEASE_ENTROPY.hex())
+    rec = {"set": setname + "-simple", "n": n, "sig_bytes": sigb, "entropy": RELEASE_ENTROPY.hex(),
+           "msgs": [m0.hex(), m1.hex(), m2.hex()]}
+    pk1, sk1 = ref("kp").split()
+    sig0 = bytes.fromhex(ref("sign %s %s" % (sk1, hx(m0))))
+    sm1 = bytes.fromhex(ref("smsign %s %s" % (sk1, hx(m1))))
+    rc, mlen, mo = ref("open %s %s" % (pk1, sm1.hex())).split()
+    v0 = int(ref("verify %s %s %s" % (pk1, sig0.hex(), hx(m0))))
+    pk2, sk2 = ref("kp").split()
+    sig2 = bytes.fromhex(ref("sign %s %s" % (sk2, hx(m2))))
+    tail = ref("drbg 16")
+    rec.update({
+        "kp1": {"pk": pk1, "sk": sk1},
+        "sig0": {"sha256": hashlib.sha256(sig0).hexdigest(), "head": sig0[:64].hex(), "verify": v0},
+        "sm1": {"sha256": hashlib.sha256(sm1).hexdigest(), "open_rc": int(rc), "open_mlen": int(mlen),
+                "open_msg": mo if mo != "-" else ""},
+        "kp2": {"pk": pk2, "sk": sk2},
+        "sig2": {"sha256": hashlib.sha256(sig2).hexdigest(), "head": sig2[:64].hex()},
+        "drbg_tail16": tail,
+    })
+    ref.close()
+    with open(os.path.join(OUT, setname + "_release.json"), "w") as f:
+        json.dump(rec, f, indent=1)
+    print(setname, "release")
+
+
 if __name__ == "__main__":
-    for s in (sys.argv[1:] or SETS):
-        gen(s)
+    args = sys.argv[1:]
+    if args and args[0] == "--release":
+        for s in (args[1:] or RELEASE_SETS):
+            gen_release(s)
+    else:
+        for s in (args or SETS):
+            gen(s)

@@ -131,3 +131,52 @@ def test_reference_batched_faces():
     bad[3 * smlen.value + 100] ^= 1
     assert L.face_mhp_crypto_sign_open(out, ctypes.byref(ml), bytes(bad), smlen.value, pk.raw, num, 8) == -1
     assert out.raw[3 * mlen:4 * mlen] == bytes(mlen) and out.raw[:3 * mlen] == m[:3 * mlen]
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f", "shake256-256f", "sha256-192f"])
+def test_dropin_release_mode_matches_reference(setname):
+    """With deterministic mode off the drop-in behaves like the reference
+    built without DEBUG_MODE (oracle/build_ref.sh --release): the keypair
+    seed (3n bytes) and each optrand (n bytes) come from the DRBG in call
+    order (sign.cu:344-349, :1950-1954).  Keypairs, signatures, crypto_sign /
+    crypto_sign_open and the DRBG bytes left afterwards equal the reference's
+    recorded run."""
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, setname + "_release.json")) as f:
+        g = json.load(f)
+    L = _lib(setname)
+    L.cuspx_set_deterministic.argtypes = [ctypes.c_int]
+    m0, m1, m2 = (bytes.fromhex(x) for x in g["msgs"])
+    pkb, skb, sigb = L.crypto_sign_publickeybytes(), L.crypto_sign_secretkeybytes(), L.crypto_sign_bytes()
+    L.cuspx_set_deterministic(0)
+    try:
+        L.randombytes_init(bytes.fromhex(g["entropy"]), None, 256)
+        pk1, sk1 = ctypes.create_string_buffer(pkb), ctypes.create_string_buffer(skb)
+        assert L.crypto_sign_keypair(pk1, sk1) == 0
+        assert (pk1.raw.hex(), sk1.raw.hex()) == (g["kp1"]["pk"], g["kp1"]["sk"])
+        sig = ctypes.create_string_buffer(sigb)
+        sl = ctypes.c_size_t()
+        assert L.crypto_sign_signature(sig, ctypes.byref(sl), m0, len(m0), sk1.raw) == 0
+        assert hashlib.sha256(sig.raw).hexdigest() == g["sig0"]["sha256"]
+        sm = ctypes.create_string_buffer(sigb + len(m1))
+        smlen = ull()
+        assert L.crypto_sign(sm, ctypes.byref(smlen), m1, len(m1), sk1.raw) == 0
+        assert hashlib.sha256(sm.raw[:smlen.value]).hexdigest() == g["sm1"]["sha256"]
+        out = ctypes.create_string_buffer(smlen.value)
+        mlen = ull()
+        rc = L.crypto_sign_open(out, ctypes.byref(mlen), sm.raw, smlen.value, pk1.raw)
+        assert (rc, mlen.value) == (g["sm1"]["open_rc"], g["sm1"]["open_mlen"])
+        assert out.raw[:mlen.value].hex() == g["sm1"]["open_msg"]
+        assert L.crypto_sign_verify(sig.raw, sigb, m0, len(m0), pk1.raw) == g["sig0"]["verify"]
+        pk2, sk2 = ctypes.create_string_buffer(pkb), ctypes.create_string_buffer(skb)
+        assert L.crypto_sign_keypair(pk2, sk2) == 0
+        assert (pk2.raw.hex(), sk2.raw.hex()) == (g["kp2"]["pk"], g["kp2"]["sk"])
+        assert L.crypto_sign_signature(sig, ctypes.byref(sl), m2, len(m2), sk2.raw) == 0
+        assert hashlib.sha256(sig.raw).hexdigest() == g["sig2"]["sha256"]
+        tail = ctypes.create_string_buffer(16)
+        L.randombytes(tail, 16)
+        assert tail.raw.hex() == g["drbg_tail16"]
+    finally:
+        L.cuspx_set_deterministic(1)

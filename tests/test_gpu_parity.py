@@ -348,3 +348,58 @@ def test_long_messages_two_warp_hashing(engine, setname):
     assert want.count(-1) == 2
     got = engine.verify_batch(sid, [pk] * len(vmsgs), vmsgs, vsigs, siglens=siglens)
     assert list(got) == want
+
+
+MIB = 1 << 20
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-simple"])
+def test_megabyte_messages_vs_oracle(engine, setname):
+    """Messages of 1 MiB - 1, 1 MiB and 1 MiB + 1 bytes (the longest of the
+    served stream) beside a short one in one batch.  PRF_msg and H_msg absorb
+    the whole message (hash_sha256.cu:99-145, :200-262; hash_shake256.cu:64-77,
+    :96-130), so every signature equals the oracle's, and every verdict the
+    oracle's, with a corrupted signature and a flipped last message byte."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(1 << 20)
+    seed = bytes(rng.randrange(256) for _ in range(3 * o.p.n))
+    pk, sk = o.seed_keypair(seed)
+    msgs = [rng.randbytes(L) for L in (MIB - 1, MIB, MIB + 1, 64)]
+    sigs, st = engine.sign_batch(sid, [sk] * len(msgs), msgs)
+    assert list(st) == [0] * len(msgs)
+    for m, s in zip(msgs, sigs):
+        assert s == o.sign(m, sk), len(m)
+    bad = bytearray(sigs[1])
+    bad[rng.randrange(len(bad))] ^= 0x08
+    flipped = bytearray(msgs[2])
+    flipped[-1] ^= 0x01
+    vmsgs = msgs + [msgs[1], bytes(flipped)]
+    vsigs = list(sigs) + [bytes(bad), sigs[2]]
+    want = [o.verify(s, m, pk) for s, m in zip(vsigs, vmsgs)]
+    assert want == [0, 0, 0, 0, -1, -1]
+    assert list(engine.verify_batch(sid, [pk] * len(vmsgs), vmsgs, vsigs)) == want
+
+
+def test_null_message_slab_is_refused(engine):
+    """A one-shot call with no message buffer but a non-empty message length
+    returns CUSPX_EINVAL (nothing is read or launched); with every length 0
+    no buffer is needed."""
+    import ctypes
+    import numpy as np
+    import cuspx_gb300 as c
+    sid = engine.set_id("sha256-128f-simple")
+    z = c.set_sizes(sid)
+    _, sks = engine.keypair_batch(sid, [bytes(48)])
+    off = np.zeros(1, dtype=np.uint64)
+    sig = ctypes.create_string_buffer(z["sig"])
+    st = np.zeros(1, dtype=np.int32)
+    for ln in (5, 0):
+        lens = np.array([ln], dtype=np.uint64)
+        rc = engine.L.cuspx_sign_batch(engine.h, sid, 1, sks[0], None, off.ctypes.data, lens.ctypes.data, None, sig,
+                                       st.ctypes.data)
+        assert rc == (-1 if ln else 0), ln
+        v = np.zeros(1, dtype=np.int32)
+        rc = engine.L.cuspx_verify_batch(engine.h, sid, 1, bytes(32), None, off.ctypes.data, lens.ctypes.data,
+                                         sig, None, v.ctypes.data)
+        assert rc == (-1 if ln else 0), ln

@@ -132,3 +132,33 @@ def test_engine_without_gpu_fails_loudly():
         pytest.skip("a GPU is present")
     with pytest.raises(c.CuspxError):
         c.Engine(0)
+
+
+def test_ctypes_struct_layouts_match_the_headers(tmp_path):
+    """The Python bindings' structures have the size and field offsets the C
+    headers give them (compiled with the host C compiler)."""
+    import shutil
+    import subprocess
+    import cuspx_gb300 as c
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    cases = {"cuspx_serve_config": c.ServeConfig, "cuspx_serve_counters": c.ServeCounters,
+             "cuspx_loadgen_config": c.LoadgenConfig, "cuspx_loadgen_result": c.LoadgenResult,
+             "cuspx_loadgen_sample": c.LoadgenSample, "cuspx_tuning": c.Tuning}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "cuspx_serve.h"', "int main(void) {"]
+    for cname, py in cases.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                        text=True).stdout.splitlines())
+    for cname, py in cases.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[cname + "." + f]) == getattr(py, f).offset, (cname, f)

@@ -116,3 +116,54 @@ def test_robust_differs_from_simple(so):
     sig = r.sign(b"robust", skr)
     assert r.verify(sig, b"robust", pkr) == 0
     assert s.verify(sig, b"robust", pks) == -1
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f", "shake256-256f", "sha256-192f"])
+def test_release_mode_call_sequence(so, setname):
+    """With DEBUG_MODE off (the reference built by oracle/build_ref.sh
+    --release) the keypair seed and each optrand come from the DRBG
+    (sign.cu:344-349, :1950-1954).  The oracle, switched to that mode,
+    reproduces the reference's keypairs, signatures, crypto_sign / open and
+    the DRBG bytes left after the whole call sequence."""
+    import ctypes
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, setname + "_release.json")) as f:
+        g = json.load(f)
+    o = so.Oracle(setname)
+    L = so.lib()
+    p = ctypes.byref(o.p)
+    m0, m1, m2 = (bytes.fromhex(x) for x in g["msgs"])
+    L.spxo_set_deterministic(0)
+    try:
+        L.spxo_randombytes_init(bytes.fromhex(g["entropy"]))
+        pk1 = ctypes.create_string_buffer(o.p.pk_bytes)
+        sk1 = ctypes.create_string_buffer(o.p.sk_bytes)
+        L.spxo_crypto_sign_keypair(p, pk1, sk1)
+        assert (pk1.raw.hex(), sk1.raw.hex()) == (g["kp1"]["pk"], g["kp1"]["sk"])
+        sig = ctypes.create_string_buffer(o.p.sig_bytes)
+        siglen = ctypes.c_size_t()
+        L.spxo_crypto_sign_signature(p, sig, ctypes.byref(siglen), m0, len(m0), sk1.raw)
+        assert hashlib.sha256(sig.raw).hexdigest() == g["sig0"]["sha256"]
+        assert o.verify(sig.raw, m0, pk1.raw) == g["sig0"]["verify"] == 0
+        sm = ctypes.create_string_buffer(o.p.sig_bytes + len(m1))
+        smlen = ctypes.c_ulonglong()
+        L.spxo_crypto_sign(p, sm, ctypes.byref(smlen), m1, len(m1), sk1.raw)
+        assert hashlib.sha256(sm.raw[:smlen.value]).hexdigest() == g["sm1"]["sha256"]
+        out = ctypes.create_string_buffer(smlen.value)
+        mlen = ctypes.c_ulonglong()
+        rc = L.spxo_crypto_sign_open(p, out, ctypes.byref(mlen), sm.raw[:smlen.value], smlen.value, pk1.raw)
+        assert (rc, mlen.value) == (g["sm1"]["open_rc"], g["sm1"]["open_mlen"])
+        assert out.raw[:mlen.value].hex() == g["sm1"]["open_msg"]
+        pk2 = ctypes.create_string_buffer(o.p.pk_bytes)
+        sk2 = ctypes.create_string_buffer(o.p.sk_bytes)
+        L.spxo_crypto_sign_keypair(p, pk2, sk2)
+        assert (pk2.raw.hex(), sk2.raw.hex()) == (g["kp2"]["pk"], g["kp2"]["sk"])
+        L.spxo_crypto_sign_signature(p, sig, ctypes.byref(siglen), m2, len(m2), sk2.raw)
+        assert hashlib.sha256(sig.raw).hexdigest() == g["sig2"]["sha256"]
+        tail = ctypes.create_string_buffer(16)
+        L.spxo_randombytes(tail, 16)
+        assert tail.raw.hex() == g["drbg_tail16"]
+    finally:
+        L.spxo_set_deterministic(1)

@@ -33,7 +33,8 @@ def _device_inputs(torch, sks, msgs):
     return d_sk, d_msg, d_off, d_len
 
 
-@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-192f-simple"])
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-192f-simple", "sha256-128s-simple",
+                                     "shake256-128f-robust"])
 def test_noalloc_matches_batch_entry_point_twice(engine, setname):
     torch = pytest.importorskip("torch")
     import cuspx_gb300 as c
@@ -72,3 +73,26 @@ def test_noalloc_rejects_batches_beyond_the_scratch(engine):
     assert L.cuspx_sign_noalloc(sid, 42, p, p, p, p, None, p, p, None) == CUSPX_ETOOBIG
     assert L.cuspx_sign_noalloc(sid, 1 << 30, p, p, p, p, None, p, p, None) == CUSPX_ETOOBIG
     assert L.cuspx_sign_noalloc(99, 1, p, p, p, p, None, p, p, None) == -1
+
+
+def test_noalloc_refuses_misaligned_or_missing_buffers(engine):
+    """Pointers the kernels would read with vector loads at a misaligned
+    address, and a missing message slab, are refused before any launch."""
+    torch = pytest.importorskip("torch")
+    import cuspx_gb300 as c
+    L = _bind()
+    sid = c.set_id("sha256-128f-simple")
+    d = torch.zeros(1 << 16, dtype=torch.uint8, device="cuda")
+    p = d.data_ptr()   # 256-byte aligned
+    ok = [p, p + 1024, p + 2048, p + 3072, None, p + 4096, p + 8192]
+    for i, bump in ((0, 4), (1, 8), (2, 4), (3, 4), (5, 4), (6, 2)):
+        args = list(ok)
+        args[i] = args[i] + bump
+        assert L.cuspx_sign_noalloc(sid, 1, *args, None) == -1, (i, bump)
+    args = list(ok)
+    args[4] = p + 12288 + 4   # optrand
+    assert L.cuspx_sign_noalloc(sid, 1, *args, None) == -1
+    args = list(ok)
+    args[1] = None   # messages
+    assert L.cuspx_sign_noalloc(sid, 1, *args, None) == -1
+    torch.cuda.synchronize()

@@ -48,6 +48,8 @@ OPS_PER_CMP = 1384   # INT ops of one SHA-256 compression (64 rounds x 14 + 48 x
 SIGN_CMP_128F = 113265
 VERIFY_CMP_128F = 6400
 KEYGEN_CMP_128F = 4567   # top-layer XMSS tree: 8 leaves x 570 + 7 H
+# message hashing of a 64-B message at n = 16: PRF_msg 5 (HMAC) + H_msg 4
+MSG_CMP_64B_SIGN = 9
 
 
 def int_frac(signs, verifies, peak_ops):
@@ -122,34 +124,63 @@ def make_inputs(rank):
     return seed, msgs
 
 
-def cpu_baseline_port(seconds):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the baseline lines."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        names = [ln.split(":", 1)[1].strip() for ln in out.splitlines() if ln.strip().startswith("Model name")]
+        if names:
+            return " / ".join(dict.fromkeys(names))
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_baseline_port(seconds, verify=True):
     """The C restatement of the reference CPU path, all host cores, bounded."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import spx_oracle
     o = spx_oracle.Oracle(SET)
     threads = os.cpu_count() or 1
     done, secs = o.throughput(0, threads, MLEN, seconds)
-    vdone, vsecs = o.throughput(1, threads, MLEN, max(1.0, seconds / 4))
-    return {"value": done / secs if secs else 0.0, "unit": "sign/s", "cores": threads, "kind": "port",
-            "sample": "%d signatures of %d-B messages (%s) on %d threads in %.1f s, each worker its own key" %
-                      (done, MLEN, SET, threads, secs),
-            "verify_per_s": vdone / vsecs if vsecs else 0.0}
+    out = {"value": done / secs if secs else 0.0, "unit": "sign/s", "cores": threads, "kind": "port",
+           "cpu_model": cpu_model(),
+           "sample": "%d signatures of %d-B messages (%s) on %d threads in %.1f s, each worker its own key" %
+                     (done, MLEN, SET, threads, secs),
+           "signatures": done, "seconds": secs,
+           "compressions_per_s": (done / secs if secs else 0.0) * (SIGN_CMP_128F + MSG_CMP_64B_SIGN)}
+    if verify:
+        vdone, vsecs = o.throughput(1, threads, MLEN, max(1.0, seconds / 4))
+        out["verify_per_s"] = vdone / vsecs if vsecs else 0.0
+    return out
 
 
 def run_reference(args):
+    """The reference arm.  A step is one bounded sample: 2 s of signing 64-B
+    messages on every host core (about 670 signatures); ms_per_step is the
+    measured wall time of a step and value the median signing rate."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    per_step = []
+    per_step, step_ms = [], []
     info = None
     for i in range(args.warmup + args.steps):
-        sample_s = 2.0
-        info = cpu_baseline_port(sample_s)
+        t0 = time.perf_counter()
+        info = cpu_baseline_port(2.0, verify=False)
         if i >= args.warmup:
             per_step.append(info["value"])
+            step_ms.append((time.perf_counter() - t0) * 1e3)
     value = statistics.median(per_step)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sign/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * BATCH / value if value else None,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms),
+            "step": "one 2-s sample of signing on all host cores (%d signatures in the last)" % info["signatures"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded uniform random 64-B messages)",
             "config": {"workload": "batched SHA-256-128f-simple sign, 4096 x 64-B messages, one key",
@@ -157,7 +188,7 @@ def run_reference(args):
                        "reference_code": "C restatement of the reference CPU path (oracle/spx_oracle.c); the "
                                          "reference's own sources are absent on the GPU host"},
             "cpu_baseline": {"value": value, "unit": "sign/s", "cores": info["cores"], "kind": "port",
-                             "sample": info["sample"]},
+                             "cpu_model": info["cpu_model"], "sample": info["sample"]},
             "e2e": {"value": value, "unit": "sign/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -307,6 +338,26 @@ def main():
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_launch_scaled_to_4096")
 
+    # ---- what the kernels execute, beside the model ----
+    # The model counts the reference's structure at 1384 INT ops per
+    # compression.  This engine skips two of its parts (the FORS secret PRF
+    # and wots_sign's chain recomputation: ~6.5k of 113k compressions), and
+    # the compiler issues fewer ALU instructions per compression than the
+    # model's ops (ncu: ALU instructions of one k_leaves launch / its
+    # compressions, profiles/k_leaves_sha256-128f_pipe.json).
+    m128 = unit_model(SET)
+    executed = {"sign_compressions": m128["executed_sign"] + MSG_CMP_64B_SIGN,
+                "step_frac_of_mix_peak": value * (m128["executed_sign"] + MSG_CMP_64B_SIGN) * OPS_PER_CMP / peak_ops}
+    pfile = os.path.join(ROOT, "profiles", "k_leaves_sha256-128f_pipe.json")
+    if os.path.exists(pfile):
+        with open(pfile) as f:
+            pj = json.load(f)
+        cmps = leaf_ops / OPS_PER_CMP   # compressions of one k_leaves launch
+        executed["k_leaves_alu_instr_per_cmp"] = pj["alu_instr_per_cmp"]
+        executed["k_leaves_alu_pipe_frac"] = cmps * pj["alu_instr_per_cmp"] / (leaves * 1e-3) / peak_alu
+        executed["alu_source"] = "ALU-pipe instructions per compression from ncu (%s) x compressions/s of " \
+                                 "k_leaves / the measured ALU-only peak" % pj.get("capture", "k_leaves")
+
     # ---- batched key generation (crypto_sign_seed_keypair per item) ----
     keygen = keygen_run(c, eng, sid, z, o, flush, args.steps, args.warmup, peak_ops) if rank == 0 else None
 
@@ -370,11 +421,11 @@ def main():
 
     served = None
     if rank == 0 and not args.no_served:
-        served = served_runs(c, eng, peak_ops)
+        served = served_runs(c, eng, peak_ops, peak_alu)
     extra = {}
     if rank == 0 and not args.no_extra:
-        extra["uneven_mixed"] = uneven_mixed(c, eng)
-        extra["verify_heavy"] = verify_heavy(c, eng)
+        extra["uneven_mixed"] = uneven_mixed(c, eng, peak_ops)
+        extra["verify_heavy"] = verify_heavy(c, eng, peak_alu)
         extra["sign_sets_1024"] = sign_sets(c, eng, peak_alu, peak_ops)
 
     cpu = None
@@ -396,6 +447,8 @@ def main():
             "verify": {"value": verify_value, "unit": "verify/s", "ms_per_batch": verify_total / args.steps,
                        "roofline_frac": int_frac(0, verify_value, peak_ops)},
             "step_roofline_frac": int_frac(value, 0, peak_ops),
+            "compressions_per_s": value * (SIGN_CMP_128F + MSG_CMP_64B_SIGN),
+            "executed": executed,
             "keygen": keygen,
             "e2e": {"value": e2e_value, "unit": "sign/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_total / args.steps,
@@ -474,7 +527,34 @@ def keygen_run(c, eng, sid, z, oracle, flush, steps, warmup, peak_ops):
             "roofline_frac": v * KEYGEN_CMP_128F * OPS_PER_CMP / peak_ops}
 
 
-def served_runs(c, eng, peak_ops, seconds=2.0):
+def stream_frac(c, r, sids, wall, peak_mix, peak_alu):
+    """Fraction of the GPU's integer peak that a served stream's completed work
+    amounts to: per set, signs x sign units + verifies x verify units + the
+    message hashing units of the requests (unit_model, msg_units), each hash
+    against its own peak (SHA-256: the round mix; Keccak: the ALU pipe)."""
+    t = 0.0
+    for i, sid in enumerate(sids):
+        m = unit_model(c.set_name(sid))
+        units = r["set_sign_done"][i] * m["sign"] + r["set_verify_done"][i] * m["verify"] + r["set_msg_units"][i]
+        t += units * m["ops_per_unit"] / (peak_alu if m["hash"] == "shake256" else peak_mix)
+    return t / wall if wall > 0 else 0.0
+
+
+def check_samples(c, samples, keys):
+    """Byte-compare the load generator's sampled signatures with the oracle
+    (in parallel threads; the oracle releases the GIL)."""
+    import concurrent.futures
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import spx_oracle
+
+    def one(smp):
+        sid, kid, st, msg, sig = smp
+        return st == 0 and sig == spx_oracle.Oracle(c.set_name(sid)).sign(msg, keys[sid][kid])
+    with concurrent.futures.ThreadPoolExecutor(min(16, os.cpu_count() or 1)) as ex:
+        return all(ex.map(one, samples))
+
+
+def served_runs(c, eng, peak_ops, peak_alu, seconds=2.0):
     """Open-loop Poisson streams through the serving loop (cuspx_serve_*).
 
     served_128f: SHA-256-128f-simple only, 30% sign / 70% verify, 64 resident
@@ -510,19 +590,28 @@ def served_runs(c, eng, peak_ops, seconds=2.0):
     out["served_128f"] = pts
     names = ["sha256-128f-simple", "sha256-192f-simple", "shake256-256f-simple"]
     sids = [c.set_id(n) for n in names]
-    srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000, mem_budget=24 << 30)
+    # admission budget: device bytes of pending plus in-flight requests; at
+    # ~15 GB/s of admitted bytes when saturated, 2 GiB bounds the queue ahead
+    # of a request to ~0.15 s of work
+    budget = 2 << 30
+    srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000, mem_budget=budget)
     per = 1024 // len(sids) + 1
+    stream_keys = {}
     for s2 in sids:
         z2 = c.set_sizes(s2)
         _, sk2 = eng.keypair_batch(s2, [rng.bytes(z2["seed"]) for _ in range(per)])
+        stream_keys[s2] = sk2
         srv.add_keys(s2, sk2)
         for op in (c.OP_SIGN, c.OP_VERIFY):
             srv.prepare(op, s2)
     pts = []
     for rate in (5e3, 20e3, 50e3, 100e3, 200e3):
         r = srv.loadgen(rate, seconds, sids, per, verify_frac=0.7, min_len=16, max_len=1 << 20, corrupt_frac=0.0,
-                        seed=7 + int(rate), pool=48)
+                        seed=7 + int(rate), pool=48, sample_every=64, sample_max=12,
+                        arena_bytes=12 * ((1 << 20) + 50000))
         ms = lambda v: [round(x / 1e3, 3) for x in v]
+        frac = stream_frac(c, r, sids, r["wall_s"], peak_ops, peak_alu)
+        sample_ok = check_samples(c, r["samples"], stream_keys)
         pts.append({"rate": rate, "sign_per_s": r["sign_throughput"], "verify_per_s": r["verify_throughput"],
                     "sign_p50_ms": r["sign_p50_us"] / 1e3, "sign_p99_ms": r["sign_p99_us"] / 1e3,
                     "verify_p50_ms": r["verify_p50_us"] / 1e3, "verify_p99_ms": r["verify_p99_us"] / 1e3,
@@ -532,11 +621,89 @@ def served_runs(c, eng, peak_ops, seconds=2.0):
                         "verify_p99_ms": ms(r["verify_p99_bucket_us"])},
                     "completed": r["completed"], "refused": r["refused"], "wrong_verdicts": r["wrong_verdicts"],
                     "mean_batch": r["mean_batch"], "launch_ms_mean": r["launch_ms_mean"],
-                    "launch_ms_max": r["launch_ms_max"]})
+                    "launch_ms_max": r["launch_ms_max"], "roofline_frac": frac,
+                    "oracle_sample": {"signatures": len(r["samples"]), "identical": sample_ok}})
     srv.close()
     out["served_stream"] = {"sets": names, "keys": per * len(sids), "lengths": "log-uniform 16 B..1 MiB",
+                            "mem_budget_bytes": budget,
+                            "oracle_sample": "1 in 64 timed signs kept (up to 12 per point), byte-compared "
+                                             "with the CPU oracle",
                             "points": pts}
     return out
+
+
+# (n, h, d, a, k) per size (params.h:33-79)
+SIZES = {"128s": (16, 63, 7, 12, 14), "128f": (16, 66, 22, 6, 33), "192s": (24, 63, 7, 14, 17),
+         "192f": (24, 66, 22, 8, 33), "256s": (32, 64, 8, 14, 22), "256f": (32, 68, 17, 9, 35)}
+
+
+def expected_digit_sum(n, samples=20000):
+    """E[sum of the len = 2n + 3 WOTS+ digits] of a uniformly random message
+    (chain_lengths, wots.cu:84-166: 2n message digits, then the checksum
+    sum(15 - d) shifted left by 4 and read as its three top 4-bit digits)."""
+    import numpy as np
+    d = np.random.default_rng(12345).integers(0, 16, size=(samples, 2 * n))
+    csum = (15 - d).sum(axis=1)
+    return float(d.sum(axis=1).mean() + ((csum >> 8) & 15).mean() + ((csum >> 4) & 15).mean() +
+                 (csum & 15).mean())
+
+
+def unit_model(name):
+    """Hash units (SHA-256 compressions, or Keccak-f[1600] permutations for
+    SHAKE sets) of one operation of a parameter set, counted the way the
+    reference's CPU path runs it, message hashing excluded:
+      sign   = seed state (SHA-256) + FORS (per tree: the signature's secret
+               PRF, 2^a leaves of PRF + F, 2^a - 1 H; then T_k) + per layer
+               wots_sign (len PRF + sum of digits F) and a treehash of 2^h'
+               leaves (len (PRF + 15 F) + T_len) and 2^h' - 1 H
+      verify = seed state + FORS (per tree F + a H; T_k) + per layer
+               sum of (15 - digit) F, T_len and h' H
+    (sign.cu:1924-1994, :3048-3121; fors.cu:107-143, :596-631; wots.cu).
+    The digit sums are their expectation over random messages.  A thash over
+    m n-byte blocks is (22 + m n + 9) / 64 compressions after the PUB_SEED
+    midstate, or (n + 32 + m n) / 136 + 1 permutations; robust adds the mask
+    (ceil(m n / 32) MGF1 blocks of (n + 26 + 9) / 64 compressions, or
+    ceil(m n / 136) squeezing permutations).  `executed_sign` drops what this
+    engine does not recompute: the FORS secret PRF (taken from its leaf) and
+    wots_sign (the signing leaf's chain values are recorded)."""
+    parts = name.split("-")
+    shake, robust = parts[0] == "shake256", parts[2] == "robust"
+    n, h, d, a, k = SIZES[parts[1]]
+    hp, ln = h // d, 2 * n + 3
+
+    def th(m):
+        if shake:
+            return (n + 32 + m * n) // 136 + 1 + (-(-m * n // 136) if robust else 0)
+        return (22 + m * n + 9 + 63) // 64 + (-(-m * n // 32) * ((n + 26 + 9 + 63) // 64) if robust else 0)
+
+    F, H, prf = th(1), th(2), 1
+    seed = 0 if shake else 1
+    leaf = ln * (prf + 15 * F) + th(ln)
+    xmss = (1 << hp) * leaf + ((1 << hp) - 1) * H
+    sign_fixed = seed + k * (prf + (1 << a) * (prf + F) + ((1 << a) - 1) * H) + th(k) + d * xmss
+    verify_fixed = seed + k * (F + a * H) + th(k) + d * (th(ln) + hp * H)
+    e = expected_digit_sum(n)
+    wots_sign = d * (ln * prf + e * F)
+    return {"unit": "perm" if shake else "cmp", "ops_per_unit": 4560 if shake else OPS_PER_CMP,
+            "sign": sign_fixed + wots_sign, "verify": verify_fixed + d * (ln * 15 - e) * F,
+            "sign_fixed": sign_fixed, "verify_fixed": verify_fixed, "wots_sign": wots_sign,
+            "verify_chain_steps": d * (ln * 15 - e), "F": F,
+            "executed_sign": sign_fixed - k * prf, "hash": "shake256" if shake else "sha256"}
+
+
+def msg_units(name, op, mlen):
+    """Hash units of the message hashing of one request: H_msg for verify,
+    PRF_msg and H_msg for sign (hash_sha256.cu:99-145, :200-262;
+    hash_shake256.cu:64-77, :96-130)."""
+    parts = name.split("-")
+    n, h, d, a, k = SIZES[parts[1]]
+    hp = h // d
+    dgst = (k * a + 7) // 8 + (hp * (d - 1) + 7) // 8 + (hp + 7) // 8
+    if parts[0] == "shake256":
+        hm = (3 * n + mlen) // 136 + 1
+        return hm if op == "verify" else hm + (2 * n + mlen) // 136 + 1
+    hm = (3 * n + mlen + 9 + 63) // 64 + (dgst + 31) // 32
+    return hm if op == "verify" else hm + 3 + (n + mlen + 9 + 63) // 64
 
 
 def leaf_units(name):
@@ -605,10 +772,12 @@ def sign_sets(c, eng, peak_alu, peak_mix, count=1024, mlen=256):
     return out
 
 
-def uneven_mixed(c, eng, reps=3):
+def uneven_mixed(c, eng, peak_mix, reps=3):
     """Uneven batch: 256 distinct keypairs (128 per set), 2048 sign requests,
     lengths floor(exp(U(ln 1, ln 65536))) B, sets SHA-256-128s-simple and
-    SHA-256-192f-robust drawn 50/50, autotuned mapping, one graph launch."""
+    SHA-256-192f-robust drawn 50/50, one graph launch; each set's mapping is
+    tuned on its own part of this very batch (its count and lengths) and
+    installed in the library for that batch size."""
     import numpy as np
     from cuspx_gb300 import autotune
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -622,7 +791,6 @@ def uneven_mixed(c, eng, reps=3):
         z = c.set_sizes(sid)
         pks, sks = eng.keypair_batch(sid, [rng.bytes(z["seed"]) for _ in range(128)])
         keys[sid] = sks
-        tuned[n] = autotune.tune(eng, sid, c.OP_SIGN, count=1024, mlen=64)[0]
     set_ids, sks, msgs = [], [], []
     for _ in range(2048):
         sid = sids[int(rng.integers(0, 2))]
@@ -630,6 +798,9 @@ def uneven_mixed(c, eng, reps=3):
         set_ids.append(sid)
         sks.append(keys[sid][int(rng.integers(0, 128))])
         msgs.append(rng.bytes(L))
+    for n, sid in zip(names, sids):
+        part = [m for s2, m in zip(set_ids, msgs) if s2 == sid]
+        tuned[n] = autotune.tune(eng, sid, c.OP_SIGN, msgs=part, use_cache=False, passes=1)[0]
     ms = c.MixedSigner(eng)
     sigs, st, _ = ms.sign(set_ids, sks, msgs)
     times = []
@@ -644,13 +815,18 @@ def uneven_mixed(c, eng, reps=3):
         o = spx_oracle.Oracle(c.set_name(set_ids[i]))
         ok &= sigs[i] == o.sign(msgs[i], sks[i])
     best = min(times)
+    units = sum(unit_model(c.set_name(s2))["sign"] + msg_units(c.set_name(s2), "sign", len(m))
+                for s2, m in zip(set_ids, msgs))
     return {"workload": "2048 sign requests, 256 keys, lengths log-uniform 1 B..64 KiB, sets %s 50/50, one "
                         "graph launch" % "+".join(names),
             "sign_per_s": 2048 / (best / 1e3), "ms_per_launch": best, "tuning": tuned,
+            "tuned_on": "each set's own part of this batch (its count and message lengths)",
+            "compressions_per_launch": units,
+            "roofline_frac": units * OPS_PER_CMP / (best * 1e-3) / peak_mix,
             "oracle_subset_identical": bool(ok), "subset": len(chk)}
 
 
-def verify_heavy(c, eng, reps=3):
+def verify_heavy(c, eng, peak_alu, reps=3):
     """16384 SHAKE-256-256f signatures (simple and robust) over 256-B
     messages, 10% with one seeded random byte xored with a nonzero byte; every
     verdict must be the expected one and a subset must match the CPU oracle."""
@@ -699,7 +875,10 @@ def verify_heavy(c, eng, reps=3):
         oracle_ok = all(o.verify(sigs[i * z["sig"]:(i + 1) * z["sig"]].tobytes(), msgs[i].tobytes(),
                                  pks[int(kidx[i])]) == int(v[i]) for i in sub)
         best = min(times[1:])
+        perms = count * (unit_model(name)["verify"] + msg_units(name, "verify", 256))
         out[name] = {"verify_per_s": count / (best / 1e3), "ms_per_launch": best, "corrupted": int(bad.sum()),
+                     "permutations_per_s": perms / (best * 1e-3),
+                     "roofline_frac": perms * 4560 / (best * 1e-3) / peak_alu,
                      "all_verdicts_expected": bool((v == expect).all()), "oracle_subset_agrees": bool(oracle_ok),
                      "oracle_subset": len(sub)}
     return out
@@ -787,7 +966,54 @@ def plain_path(c):
                         "call at a time through libspx_%s.so" % SET,
             "sign_per_s": 1e3 * len(s_lat) / sum(s_lat), "verify_per_s": 1e3 * len(v_lat) / sum(v_lat),
             "sign_ms_p50": statistics.median(s_lat), "verify_ms_p50": statistics.median(v_lat),
-            "keypair_ms": kp_ms, "keypair_note": "median of 5 calls after a first (context-creating) call"}
+            "keypair_ms": kp_ms, "keypair_note": "median of 5 calls after a first (context-creating) call",
+            "threads8": threaded_dropin(L, sk.raw, pk.raw, msgs)}
+
+
+def threaded_dropin(L, sk, pk, msgs, nthreads=8, seconds=1.0):
+    """The same drop-in called from 8 host threads at once, each looping over
+    crypto_sign_signature (then crypto_sign_verify) for about a second:
+    concurrent calls share launches.  Python threads run the calls in
+    parallel because ctypes releases the GIL during each call."""
+    import ctypes
+    import threading
+
+    def run(fn):
+        counts = [0] * nthreads
+        barrier = threading.Barrier(nthreads + 1)
+        stop = [False]
+
+        def worker(t):
+            sig = ctypes.create_string_buffer(17088)
+            sl = ctypes.c_size_t()
+            barrier.wait()
+            i = t
+            while not stop[0]:
+                fn(sig, sl, msgs[i % len(msgs)])
+                counts[t] += 1
+                i += 1
+
+        ths = [threading.Thread(target=worker, args=(t,)) for t in range(nthreads)]
+        for th in ths:
+            th.start()
+        barrier.wait()
+        t0 = time.perf_counter()
+        time.sleep(seconds)
+        stop[0] = True
+        for th in ths:
+            th.join()
+        return sum(counts) / (time.perf_counter() - t0)
+
+    sigs = {}
+    for m in msgs:
+        sig = ctypes.create_string_buffer(17088)
+        sl = ctypes.c_size_t()
+        L.crypto_sign_signature(sig, ctypes.byref(sl), m, len(m), sk)
+        sigs[m] = sig.raw
+    sign_rate = run(lambda sig, sl, m: L.crypto_sign_signature(sig, ctypes.byref(sl), m, len(m), sk))
+    verify_rate = run(lambda sig, sl, m: L.crypto_sign_verify(sigs[m], 17088, m, len(m), pk))
+    return {"threads": nthreads, "sign_per_s": sign_rate, "verify_per_s": verify_rate,
+            "note": "api.h calls from 8 threads at once; concurrent one-shot calls are combined into shared launches"}
 
 
 if __name__ == "__main__":

@@ -27,7 +27,9 @@ EXPORTS = [
     "cuspx_batch_download", "cuspx_batch_download_async", "cuspx_batch_sync", "cuspx_batch_last_ms", "cuspx_batch_stream",
     "cuspx_batch_device_ptrs", "cuspx_batch_profile", "cuspx_batch_kernel_ms",
     "cuspx_randombytes_init", "cuspx_randombytes", "cuspx_aes256_ecb", "cuspx_set_deterministic",
-    "cuspx_deterministic", "cuspx_int_peak", "cuspx_int_peak_mix",
+    "cuspx_deterministic", "cuspx_int_peak", "cuspx_int_peak_mix", "cuspx_cmp_rate",
+    "cuspx_set_tuning_for", "cuspx_get_tuning_for", "cuspx_clear_tuning_for", "cuspx_load_tuning",
+    "cuspx_device_name",
 ]
 
 
@@ -39,7 +41,7 @@ class Tuning(ctypes.Structure):
     """cuspx_tuning: the launch mapping of one parameter set."""
     _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
                                             "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode",
-                                            "chain_mode_max", "verify_slots")]
+                                            "chain_mode_max", "verify_slots", "verify_item_max")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -96,6 +98,12 @@ def lib():
     L.cuspx_set_deterministic.restype = None
     L.cuspx_int_peak.argtypes = [c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
     L.cuspx_int_peak_mix.argtypes = [c.c_int, c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
+    L.cuspx_cmp_rate.argtypes = [c.c_int, c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double)]
+    L.cuspx_set_tuning_for.argtypes = [vp, c.c_int, c.c_int, sz, c.POINTER(Tuning)]
+    L.cuspx_get_tuning_for.argtypes = [vp, c.c_int, c.c_int, sz, c.POINTER(Tuning)]
+    L.cuspx_clear_tuning_for.argtypes = [vp, c.c_int, c.c_int]
+    L.cuspx_load_tuning.argtypes = [vp, c.c_char_p]
+    L.cuspx_device_name.argtypes = [c.c_int, c.c_char_p, sz]
     _lib = L
     return L
 
@@ -191,7 +199,7 @@ class Engine:
 
     def set_tuning(self, sid, **kw):
         """Change fields of a set's launch mapping (others keep their value)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")
@@ -200,6 +208,30 @@ class Engine:
         t = Tuning()
         self._check(self.L.cuspx_get_tuning(self.h, sid, ctypes.byref(t)), "get_tuning")
         return t.as_dict()
+
+    def set_tuning_for(self, sid, op, max_count, **kw):
+        """Mapping of (set, op) for batches of at most max_count items (fields
+        not given keep the set's base mapping)."""
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1)
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(self.L.cuspx_set_tuning_for(self.h, sid, op, max_count, ctypes.byref(t)), "set_tuning_for")
+
+    def get_tuning_for(self, sid, op, count):
+        """The mapping a batch of `count` items of (set, op) runs with."""
+        t = Tuning()
+        self._check(self.L.cuspx_get_tuning_for(self.h, sid, op, count, ctypes.byref(t)), "get_tuning_for")
+        return t.as_dict()
+
+    def clear_tuning_for(self, sid, op=-1):
+        self._check(self.L.cuspx_clear_tuning_for(self.h, sid, op), "clear_tuning_for")
+
+    def load_tuning(self, path):
+        """Install a tuning file's entries for this GPU; returns how many."""
+        rc = self.L.cuspx_load_tuning(self.h, path.encode())
+        if rc < 0:
+            raise CuspxError("load_tuning(%s) failed (%d)" % (path, rc))
+        return rc
 
     def keypair_batch(self, sid, seeds):
         z = set_sizes(sid)
@@ -344,6 +376,24 @@ def int_peak(device=0, iters=4096, mix=0):
     if rc != 0:
         raise CuspxError("cuspx_int_peak_mix failed (%d)" % rc)
     return ops.value, ms.value
+
+
+def device_name(device=0):
+    buf = ctypes.create_string_buffer(256)
+    if lib().cuspx_device_name(device, buf, 256) != 0:
+        raise CuspxError("no CUDA device %d" % device)
+    return buf.value.decode()
+
+
+def cmp_rate(warps_per_sm, device=0, iters=2048):
+    """(SHA-256 compressions/s over all SMs, ns per compression of one lane's
+    dependent chain) with warps_per_sm warps on every SM."""
+    r = ctypes.c_double()
+    ns = ctypes.c_double()
+    rc = lib().cuspx_cmp_rate(device, warps_per_sm, iters, ctypes.byref(r), ctypes.byref(ns))
+    if rc != 0:
+        raise CuspxError("cuspx_cmp_rate failed (%d)" % rc)
+    return r.value, ns.value
 
 
 def dropin_path(set_name):

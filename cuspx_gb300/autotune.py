@@ -1,28 +1,34 @@
-"""Per-parameter-set launch-mapping autotuner.
+"""Per-parameter-set, per-batch-size launch-mapping autotuner.
 
 The reference fixes its mapping at compile time (all_option.h:7-68:
 HP_PARALLELISM, block-size and load-balancing switches).  Here the mapping is
-a runtime cuspx_tuning per parameter set, and this module picks it by timing
-real batches on the device:
+a runtime cuspx_tuning per parameter set, refined per (operation, batch-size
+bucket), and this module picks it by timing real batches on the device:
 
   sign:   chain_mode_max (lane per chain vs lane per leaf for this batch
           size), fors_lanes_log2 (lanes per FORS tree), tree_mode,
           leaf_block, fors_block, tree_warps
-  verify: verify_mode (layered kernels or one persistent launch), and for
+  verify: verify_item_max (one item per block at this size or not),
+          verify_mode (layered kernels or one persistent launch), and for
           each the chains per warp / items per warp and block size
 
 Search is coordinate descent: each knob is swept with the others held, the
 best value kept, for two passes.  Every candidate is timed with CUDA events
-on the batch stream (min of `reps` runs after a warm-up).  Results are cached
-per (GPU name, set, op, batch-size bucket) in a JSON file
-($CUSPX_TUNE_CACHE, default ~/.cache/cuspx/tune.json).
+on the batch stream (min of `reps` runs after a warm-up).
+
+The result is installed in the library, not only in Python: the engine gets
+a per-size entry (cuspx_set_tuning_for) for batches of up to the bucket's
+size, and the result is appended to a tab-separated tuning file
+($CUSPX_TUNE_CACHE, default ~/.cache/cuspx/tune.tsv), one line per
+(GPU name, set, op, bucket).  cuspx_create reads that file, so every later
+context -- the api.h drop-ins, the one-shot calls and the serving loop
+included -- runs the tuned mappings without Python.
 """
-import json
 import os
 
 import numpy as np
 
-from . import OP_SIGN, OP_VERIFY, pack_messages, set_name, set_sizes
+from . import OP_SIGN, OP_VERIFY, device_name, pack_messages, set_name, set_sizes
 
 SIGN_SPACE = {
     "chain_mode_max": [0, 256],
@@ -33,46 +39,56 @@ SIGN_SPACE = {
     "tree_warps": [1, 2, 4],
 }
 VERIFY_SPACE = {
+    "verify_item_max": [0, None],   # None: this bucket's size (one item per block)
     "verify_mode": [0, 1, 2],
     "verify_slots": [2, 3, 4, 6, 8],
     "chains_per_warp": [32, 64, 128, 256, 512],
     "verify_block": [32, 64, 128],
 }
+OP_NAMES = {OP_SIGN: "sign", OP_VERIFY: "verify"}
 
 
-def _cache_path():
-    return os.environ.get("CUSPX_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "cuspx", "tune.json"))
+def cache_path():
+    return os.environ.get("CUSPX_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "cuspx", "tune.tsv"))
 
 
-def _gpu_name():
-    try:
-        import torch
-        return torch.cuda.get_device_name(0)
-    except Exception:
-        return "gpu"
-
-
-def _bucket(n):
+def bucket(n):
+    """Batch-size bucket: the power of 4 at or above n."""
     b = 1
     while b < n:
         b *= 4
     return b
 
 
-def _load_cache():
+def load_cache(path=None):
+    """{(gpu, set, op, bucket): (ms, mapping)} from the tuning file."""
+    out = {}
     try:
-        with open(_cache_path()) as f:
-            return json.load(f)
+        with open(path or cache_path()) as f:
+            for line in f:
+                col = line.rstrip("\n").split("\t")
+                if len(col) != 6:
+                    continue
+                mapping = dict((k, int(v)) for k, v in (kv.split("=") for kv in col[5].split(",") if kv))
+                out[(col[0], col[1], col[2], int(col[3]))] = (float(col[4]), mapping)
     except (OSError, ValueError):
-        return {}
+        pass
+    return out
 
 
-def _save_cache(c):
-    p = _cache_path()
+def save_entry(key, ms, mapping, path=None):
+    """Write (or replace) one line of the tuning file."""
+    path = path or cache_path()
+    cache = load_cache(path)
+    cache[key] = (ms, mapping)
     try:
-        os.makedirs(os.path.dirname(p), exist_ok=True)
-        with open(p, "w") as f:
-            json.dump(c, f, indent=1)
+        os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            for (gpu, sname, op, b), (m, mp) in sorted(cache.items()):
+                f.write("%s\t%s\t%s\t%d\t%.4f\t%s\n" % (gpu, sname, op, b, m,
+                                                        ",".join("%s=%d" % kv for kv in sorted(mp.items()))))
+        os.replace(tmp, path)
     except OSError:
         pass
 
@@ -89,18 +105,25 @@ def _time(batch, reps):
     return best
 
 
-def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, reps=2, passes=2, use_cache=True, verbose=False):
-    """Pick and install the fastest mapping of `op` for set `sid` at `count`
-    items of `mlen`-byte messages.  Returns (mapping dict, best ms)."""
-    key = "%s|%s|%s|%d" % (_gpu_name(), set_name(sid), "sign" if op == OP_SIGN else "verify", _bucket(count))
-    cache = _load_cache() if use_cache else {}
-    if key in cache:
-        eng.set_tuning(sid, **cache[key]["mapping"])
-        return cache[key]["mapping"], cache[key]["ms"]
+def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2, use_cache=True, verbose=False):
+    """Pick the fastest mapping of `op` for set `sid` on a batch of `count`
+    `mlen`-byte random messages, or on the given `msgs` (their count and
+    lengths), install it in the engine for that batch-size bucket and record
+    it in the tuning file.  Returns (mapping dict, best ms)."""
+    if msgs is not None:
+        count = len(msgs)
+    b = bucket(count)
+    key = (device_name(), set_name(sid), OP_NAMES[op], b)
+    if use_cache:
+        hit = load_cache().get(key)
+        if hit:
+            eng.set_tuning_for(sid, op, b, **hit[1])
+            return hit[1], hit[0]
     z = set_sizes(sid)
     rng = np.random.default_rng(1234)
     pks, sks = eng.keypair_batch(sid, [rng.bytes(z["seed"])])
-    msgs = [rng.bytes(mlen) for _ in range(count)]
+    if msgs is None:
+        msgs = [rng.bytes(mlen) for _ in range(count)]
     slab, offs, lens = pack_messages(msgs)
     kidx = np.zeros(count, dtype=np.uint32)
     sb = eng.batch(OP_SIGN, sid, count, len(slab), 1)
@@ -113,8 +136,10 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, reps=2, passes=2, use_cache=
         vb = eng.batch(OP_VERIFY, sid, count, len(slab), 1)
         vb.upload(count, pks[0], 1, kidx, slab, len(slab), offs, lens, sigs)
         batch = vb
-    space = SIGN_SPACE if op == OP_SIGN else VERIFY_SPACE
-    cur = {k: v for k, v in eng.get_tuning(sid).items() if k in space}
+    space = {k: [b if v is None else v for v in vals]
+             for k, vals in (SIGN_SPACE if op == OP_SIGN else VERIFY_SPACE).items()}
+    cur = {k: v for k, v in eng.get_tuning_for(sid, op, count).items() if k in space}
+    eng.set_tuning_for(sid, op, b, **cur)
     best_ms = _time(batch, reps)
     for _ in range(passes):
         improved = False
@@ -123,21 +148,19 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, reps=2, passes=2, use_cache=
                 if v == cur[knob]:
                     continue
                 trial = dict(cur, **{knob: v})
-                eng.set_tuning(sid, **trial)
+                eng.set_tuning_for(sid, op, b, **trial)
                 ms = _time(batch, reps)
                 if verbose:
                     print("  %s=%s %.3f ms" % (knob, v, ms))
                 if ms < best_ms * 0.995:
                     best_ms, cur, improved = ms, trial, True
-            eng.set_tuning(sid, **cur)
+            eng.set_tuning_for(sid, op, b, **cur)
         if not improved:
             break
-    eng.set_tuning(sid, **cur)
+    eng.set_tuning_for(sid, op, b, **cur)
     batch.close()
     if op == OP_VERIFY:
         sb.close()
     if use_cache:
-        cache = _load_cache()
-        cache[key] = {"mapping": cur, "ms": best_ms, "count": count, "mlen": mlen}
-        _save_cache(cache)
+        save_entry(key, best_ms, cur)
     return cur, best_ms

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "../../include/cuspx.h"
+#include "spx_hash.cuh"
 
 namespace {
 
@@ -45,7 +46,58 @@ __global__ void k_int_mix(uint32_t *out, int iters, uint32_t seed) {
     if (acc == 0x12345678u) out[0] = acc;  // keeps the chains live
 }
 
+// Each thread runs `iters` SHA-256 compressions in a dependent chain (every
+// block is built from the previous state), like one lane of a verify task:
+// with one warp per SM this is the latency of a compression, with more it
+// shows how many warps an SM needs before the ALU pipe, not the round's
+// dependency chain, sets the rate.
+__global__ void k_cmp_chain(uint32_t *out, int iters, uint32_t seed) {
+    uint32_t st[8], w[16];
+#pragma unroll
+    for (int i = 0; i < 8; i++) st[i] = seed * (threadIdx.x + 1) + i * 0x9e3779b9u + blockIdx.x;
+#pragma unroll
+    for (int i = 0; i < 16; i++) w[i] = seed ^ (i * 0x7f4a7c15u) ^ threadIdx.x;
+    for (int it = 0; it < iters; it++) {
+        uint32_t m[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) m[i] = w[i] ^ st[i & 7];
+        cuspx::sha256_compress(st, m);
+    }
+    uint32_t acc = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc ^= st[i];
+    if (acc == 0x12345678u) out[0] = acc;  // keeps the chain live
+}
+
 }  // namespace
+
+extern "C" int cuspx_cmp_rate(int device, int warps_per_sm, int iters, double *cmp_per_s, double *ns_per_cmp) {
+    if (!cmp_per_s || iters <= 0 || warps_per_sm < 1 || warps_per_sm > 32) return CUSPX_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return CUSPX_ECUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    // one block per SM, so every SM holds exactly warps_per_sm warps
+    const int threads = 32 * warps_per_sm, blocks = sms;
+    uint32_t *out = nullptr;
+    if (cudaMalloc(&out, 4) != cudaSuccess) return CUSPX_ECUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_cmp_chain<<<blocks, threads>>>(out, iters / 8 + 1, 1u);  // warm-up
+    cudaEventRecord(e0);
+    k_cmp_chain<<<blocks, threads>>>(out, iters, 1u);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return CUSPX_ECUDA;
+    *cmp_per_s = (double)blocks * threads * iters / (ms * 1e-3);
+    if (ns_per_cmp) *ns_per_cmp = ms * 1e6 / iters;
+    return CUSPX_OK;
+}
 
 extern "C" int cuspx_int_peak_mix(int device, int iters, int mix, double *ops_per_s, float *ms_out) {
     if (!ops_per_s || iters <= 0 || (mix != 0 && mix != 1)) return CUSPX_EINVAL;

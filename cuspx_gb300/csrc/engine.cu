@@ -8,9 +8,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -87,11 +89,29 @@ static const size_t kKeygenChainItems = 16384;
 // two-warp message kernels of the SHA-256 sets
 static const uint64_t kPairMsgBytes = 2048;
 
+struct OneshotJob;
+
+// a tuned mapping for batches of at most max_count items of one (set, op)
+struct TuneEntry {
+    size_t max_count;
+    Tuning t;
+};
+constexpr int kMaxTuneEntries = 16;
+
 struct cuspx_ctx {
     int device = 0;
+    std::mutex err_mu;   // err is written by any calling thread
     std::string err;
     Tuning tune[kNumSets];
+    // per-size entries (sorted by max_count) that take precedence over tune[]
+    TuneEntry tune_for[kNumSets][3][kMaxTuneEntries];
+    int ntune_for[kNumSets][3] = {};
     bool configured[2][3][2] = {};
+    // one-shot calls: queued jobs and whether a caller is running a launch
+    std::mutex comb_mu;
+    std::condition_variable comb_cv;
+    std::deque<OneshotJob *> comb_q;
+    bool comb_busy = false;
     std::mutex mu;       // one-shot batches
     std::mutex cfg_mu;   // kernel attribute configuration
     cuspx_batch *oneshot[3][kNumSets] = {};
@@ -123,6 +143,7 @@ struct cuspx_batch {
     SetParams P{};
     size_t cap = 0, msg_cap = 0, key_cap = 0;
     cudaStream_t s = nullptr;
+    bool own_stream = true;    // false: s belongs to the caller (batch_share_stream)
     StreamFork fork{};         // sign batches: FORS beside the hypertree
     uint8_t *keys = nullptr;
     uint32_t *keyrow = nullptr;
@@ -177,7 +198,10 @@ struct cuspx_batch {
 };
 
 static int fail(cuspx_ctx *ctx, int code, const std::string &msg) {
-    if (ctx) ctx->err = msg;
+    if (ctx) {
+        std::lock_guard<std::mutex> lk(ctx->err_mu);
+        ctx->err = msg;
+    }
     return code;
 }
 
@@ -192,6 +216,19 @@ static int cuda_fail(cuspx_ctx *ctx, cudaError_t e, const char *what) {
         cudaError_t _e = (call);                              \
         if (_e != cudaSuccess) return cuda_fail(ctx, _e, #call); \
     } while (0)
+
+// The mapping a batch of `count` items of (set, op) runs with: the per-size
+// entry with the smallest max_count >= count (the largest entry for bigger
+// batches), else the set's base mapping.
+static const Tuning &effective_tuning(const cuspx_ctx *ctx, int set, int op, size_t count) {
+    const int ne = ctx->ntune_for[set][op];
+    if (ne == 0) return ctx->tune[set];
+    for (int i = 0; i < ne; i++)
+        if (count <= ctx->tune_for[set][op][i].max_count) return ctx->tune_for[set][op][i].t;
+    return ctx->tune_for[set][op][ne - 1].t;
+}
+
+static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet);
 
 extern "C" {
 
@@ -250,10 +287,23 @@ int cuspx_create(int device, cuspx_ctx **out) {
         // 4 slots 98.9 ms; 4096 SHA-256-192f-robust 11.9 / 12.8 ms), except
         // robust SHA-256 at n = 32 (4096 SHA-256-256f-robust 22.8 / 21.1 ms)
         if (sd.robust && !(sd.hash == 0 && sd.n == 32)) t.verify_slots = 2;
+        // one item per block up to 128 items: SHA-256-128f 1 item 0.98 ms
+        // against 1.18 ms persistent, 128 items 1.00 / 1.20 ms, 256 items
+        // 1.44 / 1.22 ms (SHAKE-256f and robust SHA-256-192f cross over
+        // between 64 and 256 as well)
+        t.verify_item_max = 128;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;
         return CUSPX_ECUDA;
+    }
+    // tuned mappings from the autotuner's file, if there is one for this GPU
+    {
+        const char *tp = getenv("CUSPX_TUNE_CACHE");
+        std::string path;
+        if (tp && *tp) path = tp;
+        else if (const char *home = getenv("HOME")) path = std::string(home) + "/.cache/cuspx/tune.tsv";
+        if (!path.empty()) load_tuning_file(c, path.c_str(), true);
     }
     // the one-shot calls' pinned staging, so that the first call does not
     // pay for the allocation (it grows on demand for larger batches)
@@ -280,11 +330,22 @@ void cuspx_destroy(cuspx_ctx *ctx) {
     delete ctx;
 }
 
-const char *cuspx_error(const cuspx_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+// the context's last failure, copied for the calling thread (another thread
+// may record a new one meanwhile)
+const char *cuspx_error(const cuspx_ctx *ctx) {
+    if (!ctx) return "null context";
+    static thread_local std::string copy;
+    cuspx_ctx *c = const_cast<cuspx_ctx *>(ctx);
+    std::lock_guard<std::mutex> lk(c->err_mu);
+    copy = c->err;
+    return copy.c_str();
+}
 
-int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
-    if (!ctx || !in || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
-    Tuning t = ctx->tune[set];
+}  // extern "C"
+
+// base with the fields of `in` applied (cuspx_set_tuning's rules)
+static int merge_tuning(cuspx_ctx *ctx, const Tuning &base, const cuspx_tuning *in, Tuning &out) {
+    Tuning t = base;
     auto blk = [&](int v, int &dst, const char *what) -> bool {
         if (v <= 0) return true;
         if (v % 32 || v > 1024) {
@@ -323,14 +384,51 @@ int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
         if (in->verify_slots > 8) return fail(ctx, CUSPX_EINVAL, "verify_slots must be in 1..8");
         t.verify_slots = in->verify_slots;
     }
+    if (in->verify_item_max >= 0) t.verify_item_max = in->verify_item_max;
+    out = t;
+    return CUSPX_OK;
+}
+
+extern "C" {
+
+int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
+    if (!ctx || !in || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
     std::lock_guard<std::mutex> lk(ctx->mu);
+    Tuning t;
+    if (int rc = merge_tuning(ctx, ctx->tune[set], in, t)) return rc;
     ctx->tune[set] = t;   // batches re-capture their graph when the mapping changed
     return CUSPX_OK;
 }
 
-int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
-    if (!ctx || !out || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
-    const Tuning &t = ctx->tune[set];
+int cuspx_set_tuning_for(cuspx_ctx *ctx, int set, int op, size_t max_count, const cuspx_tuning *in) {
+    if (!ctx || !in || set < 0 || set >= kNumSets || op < 0 || op > 2 || max_count == 0) return CUSPX_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Tuning t;
+    if (int rc = merge_tuning(ctx, ctx->tune[set], in, t)) return rc;
+    TuneEntry *e = ctx->tune_for[set][op];
+    int &ne = ctx->ntune_for[set][op];
+    int i = 0;
+    while (i < ne && e[i].max_count < max_count) i++;
+    if (i < ne && e[i].max_count == max_count) {
+        e[i].t = t;
+        return CUSPX_OK;
+    }
+    if (ne == kMaxTuneEntries) return fail(ctx, CUSPX_ENOMEM, "set_tuning_for: 16 entries per set and op");
+    for (int j = ne; j > i; j--) e[j] = e[j - 1];
+    e[i] = TuneEntry{max_count, t};
+    ne++;
+    return CUSPX_OK;
+}
+
+int cuspx_clear_tuning_for(cuspx_ctx *ctx, int set, int op) {
+    if (!ctx || set < 0 || set >= kNumSets || op > 2) return CUSPX_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    for (int o = 0; o < 3; o++)
+        if (op < 0 || o == op) ctx->ntune_for[set][o] = 0;
+    return CUSPX_OK;
+}
+
+static void to_abi(const Tuning &t, cuspx_tuning *out) {
     out->leaf_block = t.leaf_block;
     out->fors_block = t.fors_block;
     out->verify_block = t.verify_block;
@@ -341,8 +439,111 @@ int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
     out->tree_mode = t.tree_mode;
     out->chain_mode_max = t.chain_mode_max;
     out->verify_slots = t.verify_slots;
+    out->verify_item_max = t.verify_item_max;
+}
+
+int cuspx_get_tuning_for(cuspx_ctx *ctx, int set, int op, size_t count, cuspx_tuning *out) {
+    if (!ctx || !out || set < 0 || set >= kNumSets || op < 0 || op > 2) return CUSPX_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    to_abi(effective_tuning(ctx, set, op, count), out);
     return CUSPX_OK;
 }
+
+int cuspx_load_tuning(cuspx_ctx *ctx, const char *path) {
+    if (!ctx || !path) return CUSPX_EINVAL;
+    return load_tuning_file(ctx, path, false);
+}
+
+int cuspx_device_name(int device, char *buf, size_t len) {
+    if (!buf || len == 0) return CUSPX_EINVAL;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        cudaGetLastError();
+        return CUSPX_ECUDA;
+    }
+    snprintf(buf, len, "%s", prop.name);
+    return CUSPX_OK;
+}
+
+int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
+    if (!ctx || !out || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
+    to_abi(ctx->tune[set], out);
+    return CUSPX_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// tuning file (written by cuspx_gb300/autotune.py): one entry per line,
+//   <gpu name> TAB <set name> TAB <sign|verify|keygen> TAB <max_count> TAB <ms> TAB <knob>=<v>,<knob>=<v>...
+// Lines of another GPU, unknown sets or knobs, and malformed lines are skipped.
+// ---------------------------------------------------------------------------
+static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
+    FILE *f = fopen(path, "r");
+    if (!f) return quiet ? 0 : fail(ctx, CUSPX_EINVAL, std::string("load_tuning: cannot open ") + path);
+    char gpu[256] = {0};
+    if (cuspx_device_name(ctx->device, gpu, sizeof gpu) != CUSPX_OK) {
+        fclose(f);
+        return CUSPX_ECUDA;
+    }
+    int installed = 0;
+    char line[2048];
+    while (fgets(line, sizeof line, f)) {
+        std::vector<std::string> col;
+        std::string cur;
+        for (const char *p = line; *p && *p != '\n' && *p != '\r'; p++) {
+            if (*p == '\t') {
+                col.push_back(cur);
+                cur.clear();
+            } else {
+                cur += *p;
+            }
+        }
+        col.push_back(cur);
+        if (col.size() != 6 || col[0] != gpu) continue;
+        const int set = set_by_name(col[1].c_str());
+        const int op = col[2] == "sign" ? CUSPX_OP_SIGN : col[2] == "verify" ? CUSPX_OP_VERIFY
+                                                        : col[2] == "keygen" ? CUSPX_OP_KEYGEN : -1;
+        const long long mc = atoll(col[3].c_str());
+        if (set < 0 || op < 0 || mc <= 0) continue;
+        cuspx_tuning t;
+        t.leaf_block = t.fors_block = t.verify_block = t.tree_warps = t.chains_per_warp = t.verify_slots = 0;
+        t.verify_mode = t.fors_lanes_log2 = t.tree_mode = t.chain_mode_max = t.verify_item_max = -1;
+        bool ok = true;
+        size_t at = 0;
+        const std::string &kv = col[5];
+        while (ok && at < kv.size()) {
+            size_t end = kv.find(',', at);
+            if (end == std::string::npos) end = kv.size();
+            const std::string item = kv.substr(at, end - at);
+            at = end + 1;
+            const size_t eq = item.find('=');
+            if (eq == std::string::npos) {
+                ok = false;
+                break;
+            }
+            const std::string k = item.substr(0, eq);
+            const int v = atoi(item.c_str() + eq + 1);
+            if (k == "leaf_block") t.leaf_block = v;
+            else if (k == "fors_block") t.fors_block = v;
+            else if (k == "verify_block") t.verify_block = v;
+            else if (k == "tree_warps") t.tree_warps = v;
+            else if (k == "chains_per_warp") t.chains_per_warp = v;
+            else if (k == "verify_mode") t.verify_mode = v;
+            else if (k == "fors_lanes_log2") t.fors_lanes_log2 = v;
+            else if (k == "tree_mode") t.tree_mode = v;
+            else if (k == "chain_mode_max") t.chain_mode_max = v;
+            else if (k == "verify_slots") t.verify_slots = v;
+            else if (k == "verify_item_max") t.verify_item_max = v;
+            else ok = false;
+        }
+        if (ok && cuspx_set_tuning_for(ctx, set, op, (size_t)mc, &t) == CUSPX_OK) installed++;
+    }
+    fclose(f);
+    return installed;
+}
+
+extern "C" {
 
 // ---------------------------------------------------------------------------
 // batches
@@ -438,9 +639,7 @@ int cuspx_batch_create(cuspx_ctx *ctx, int op, int set, size_t capacity, size_t 
         }
     }
     if (rc != CUSPX_OK) {
-        std::string m = ctx->err;
-        cuspx_batch_destroy(b);
-        ctx->err = m;
+        cuspx_batch_destroy(b);   // records nothing: the allocation failure's message stays
         return rc;
     }
     *out = b;
@@ -462,7 +661,7 @@ void cuspx_batch_destroy(cuspx_batch *b) {
     }
     if (b->fork.fork) cudaEventDestroy(b->fork.fork);
     if (b->fork.join) cudaEventDestroy(b->fork.join);
-    if (b->s) cudaStreamDestroy(b->s);
+    if (b->s && b->own_stream) cudaStreamDestroy(b->s);
     delete b;
 }
 
@@ -531,7 +730,7 @@ int cuspx_batch_upload(cuspx_batch *b, size_t count, const uint8_t *keys, size_t
 
 static void launch_seq(cuspx_batch *b, PhaseTimer *pt) {
     const FamilyOps &ops = family_of(b->set);
-    const Tuning &tu = b->ctx->tune[b->set];
+    const Tuning &tu = effective_tuning(b->ctx, b->set, b->op, b->count);
     const SetParams &P = b->P;
     const uint32_t cnt = (uint32_t)b->count;
     if (b->op == CUSPX_OP_SIGN) {
@@ -615,7 +814,7 @@ int cuspx_batch_run(cuspx_batch *b) {
         b->ran = true;
         return CUSPX_OK;
     }
-    const Tuning &tu = ctx->tune[b->set];
+    const Tuning &tu = effective_tuning(ctx, b->set, b->op, b->count);
     cuspx_batch::GraphKey key{b->count, b->use_keyrow, b->use_aux, b->use_siglen, b->long_msgs, b->bound_keys, tu};
     b->use_clock++;
     cuspx_batch::GraphEntry *hit = nullptr;
@@ -730,23 +929,25 @@ void batch_direct_launch(cuspx_batch *b, bool on) {
     }
 }
 
-// Library-internal: give an idle batch a stream of the given priority (lower
-// numbers run first); its captured graphs are dropped with the old stream.
-int batch_set_stream_priority(cuspx_batch *b, int priority) {
-    if (!b) return CUSPX_EINVAL;
+// Library-internal: launch an idle batch that already runs on a caller's
+// stream (batch_share_stream) on another of the caller's streams from now
+// on.  Nothing is waited for: the caller knows the batch's work is done.
+void batch_use_stream(cuspx_batch *b, cudaStream_t s) {
+    if (b && s && !b->own_stream) b->s = s;
+}
+
+// Library-internal: run an idle batch on a stream owned by the caller (which
+// keeps it alive while the batch exists and destroys it afterwards); the
+// batch's own stream and captured graphs are dropped.  Several batches may
+// share one stream: their launches then run in submission order.
+int batch_share_stream(cuspx_batch *b, cudaStream_t s) {
+    if (!b || !s) return CUSPX_EINVAL;
     CK(cudaStreamSynchronize(b->s), b->ctx);
-    cudaStream_t ns;
-    CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, priority), b->ctx);
     for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
     b->graphs.clear();
-    cudaStreamDestroy(b->s);
-    b->s = ns;
-    if (b->fork.side) {   // the FORS side stream runs at the same priority
-        CK(cudaStreamSynchronize(b->fork.side), b->ctx);
-        CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, priority), b->ctx);
-        cudaStreamDestroy(b->fork.side);
-        b->fork.side = ns;
-    }
+    if (b->own_stream) cudaStreamDestroy(b->s);
+    b->s = s;
+    b->own_stream = false;
     return CUSPX_OK;
 }
 }  // namespace cuspx
@@ -853,43 +1054,184 @@ static size_t packed_bytes(size_t count, const uint64_t *len) {
     for (size_t i = 0; i < count; i++) total += al16(len[i]);
     return total;
 }
-// pack the messages into staging: slab (total + 16 bytes, zero padding),
-// offsets and lengths
-static void pack_staged(size_t count, const uint8_t *msgs, const uint64_t *off, const uint64_t *len, size_t total,
-                        uint8_t *slab, uint64_t *noff, uint64_t *nlen) {
-    memset(slab, 0, total + 16);
-    size_t o = 0;
-    for (size_t i = 0; i < count; i++) {
-        noff[i] = o;
-        nlen[i] = len[i];
-        if (len[i]) memcpy(slab + o, msgs + off[i], len[i]);
-        o += al16(len[i]);
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// One-shot calls from concurrent threads share launches.  Each call becomes
+// a job on the context's queue; a caller that finds no launch running takes
+// the oldest job and every other queued job of the same operation and set
+// (up to kCombineItems items and kCombineBytes of messages), packs them
+// into one batch, launches it, and hands every job its slice of the results.
+// Callers arriving meanwhile queue for the next launch, so N threads calling
+// crypto_sign_signature at once share launches instead of running one
+// launch each in turn.  A lone caller sees no difference.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kCombineItems = 4096;
+constexpr size_t kCombineBytes = (size_t)256 << 20;
+}  // namespace
+
+struct OneshotJob {
+    int op = 0, set = 0;
+    size_t count = 0;
+    const uint8_t *keys = nullptr;   // seeds (keygen), sk rows (sign), pk rows (verify)
+    const uint8_t *msgs = nullptr;
+    const uint64_t *off = nullptr, *len = nullptr;
+    const uint8_t *aux = nullptr;    // sign: optrand (may be null); verify: signature rows
+    const uint64_t *siglens = nullptr;
+    uint8_t *out = nullptr;          // sign: signatures; keygen: pk rows
+    uint8_t *out2 = nullptr;         // keygen: sk rows
+    int32_t *status = nullptr;       // sign: statuses (may be null); verify: verdicts
+    size_t msg_bytes = 0;            // its messages packed at 16-byte offsets
+    int rc = CUSPX_OK;
+    bool done = false;
+};
+
+// Run jobs of one (op, set) as one batch; under ctx->mu.
+static int oneshot_run(cuspx_ctx *ctx, int op, int set, const std::vector<OneshotJob *> &jobs) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    size_t count = 0, total = 0;
+    bool any_opt = false;
+    for (const OneshotJob *j : jobs) {
+        count += j->count;
+        total += j->msg_bytes;
+        any_opt |= j->aux != nullptr;
     }
+    cuspx_batch *b;
+    int rc = oneshot_batch(ctx, op, set, count, total, &b);
+    if (rc) return rc;
+    const SetParams &P = b->P;
+    const size_t n = P.n;
+    Staging st;
+    if (op == CUSPX_OP_KEYGEN) {
+        const size_t seed_b = count * 3 * n, sk_b = count * P.sk_bytes, pk_b = count * P.pk_bytes;
+        if ((rc = oneshot_stage(ctx, al16(seed_b) + al16(sk_b) + al16(pk_b), st))) return rc;
+        uint8_t *h_seed = (uint8_t *)st.take(seed_b);
+        uint8_t *h_sk = (uint8_t *)st.take(sk_b);
+        uint8_t *h_pk = (uint8_t *)st.take(pk_b);
+        size_t at = 0;
+        for (const OneshotJob *j : jobs) {
+            memcpy(h_seed + at * 3 * n, j->keys, j->count * 3 * n);
+            at += j->count;
+        }
+        if ((rc = cuspx_batch_upload(b, count, h_seed, count, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
+                                     nullptr)))
+            return rc;
+        if ((rc = cuspx_batch_run(b))) return rc;
+        if ((rc = cuspx_batch_download(b, h_sk, h_pk, nullptr))) return rc;
+        at = 0;
+        for (const OneshotJob *j : jobs) {
+            memcpy(j->out2, h_sk + at * P.sk_bytes, j->count * P.sk_bytes);
+            memcpy(j->out, h_pk + at * P.pk_bytes, j->count * P.pk_bytes);
+            at += j->count;
+        }
+        return CUSPX_OK;
+    }
+    const bool sign = op == CUSPX_OP_SIGN;
+    const size_t key_b = count * (sign ? P.sk_bytes : P.pk_bytes);
+    const size_t opt_b = sign && any_opt ? count * n : 0;
+    const size_t sig_b = count * P.sig_bytes;
+    const size_t sl_b = sign ? 0 : count * 8;
+    if ((rc = oneshot_stage(ctx, al16(key_b) + 2 * al16(count * 8) + al16(opt_b) + al16(sl_b) + al16(total + 16) +
+                                     al16(sig_b) + al16(count * 4), st)))
+        return rc;
+    uint8_t *h_key = (uint8_t *)st.take(key_b);
+    uint64_t *h_off = (uint64_t *)st.take(count * 8);
+    uint64_t *h_len = (uint64_t *)st.take(count * 8);
+    uint8_t *h_opt = opt_b ? (uint8_t *)st.take(opt_b) : nullptr;
+    uint64_t *h_sl = sl_b ? (uint64_t *)st.take(sl_b) : nullptr;
+    uint8_t *h_msg = (uint8_t *)st.take(total + 16);
+    uint8_t *h_sig = (uint8_t *)st.take(sig_b);
+    int32_t *h_st = (int32_t *)st.take(count * 4);
+    memset(h_msg, 0, total + 16);
+    size_t at = 0, o = 0;
+    const size_t krow = sign ? P.sk_bytes : P.pk_bytes;
+    for (const OneshotJob *j : jobs) {
+        memcpy(h_key + at * krow, j->keys, j->count * krow);
+        for (size_t i = 0; i < j->count; i++) {
+            h_off[at + i] = o;
+            h_len[at + i] = j->len[i];
+            if (j->len[i]) memcpy(h_msg + o, j->msgs + j->off[i], j->len[i]);
+            o += al16(j->len[i]);
+        }
+        if (h_opt) {
+            // a job without optrand gets the reference's fixed 0xAD bytes (sign.cu:1950-1954)
+            if (j->aux) memcpy(h_opt + at * n, j->aux, j->count * n);
+            else memset(h_opt + at * n, 0xad, j->count * n);
+        }
+        if (!sign) {
+            memcpy(h_sig + at * P.sig_bytes, j->aux, j->count * P.sig_bytes);
+            for (size_t i = 0; i < j->count; i++) h_sl[at + i] = j->siglens ? j->siglens[i] : P.sig_bytes;
+        }
+        at += j->count;
+    }
+    if ((rc = cuspx_batch_upload(b, count, h_key, count, nullptr, h_msg, total, h_off, h_len,
+                                 sign ? h_opt : h_sig, h_sl)))
+        return rc;
+    if ((rc = cuspx_batch_run(b))) return rc;
+    if ((rc = cuspx_batch_download(b, sign ? h_sig : nullptr, nullptr, h_st))) return rc;
+    at = 0;
+    for (const OneshotJob *j : jobs) {
+        if (sign) memcpy(j->out, h_sig + at * P.sig_bytes, j->count * P.sig_bytes);
+        if (j->status) memcpy(j->status, h_st + at, j->count * 4);
+        at += j->count;
+    }
+    return CUSPX_OK;
 }
+
+// Queue a job and return when it has run (see above).
+static int oneshot_submit(cuspx_ctx *ctx, OneshotJob &job) {
+    std::unique_lock<std::mutex> lk(ctx->comb_mu);
+    ctx->comb_q.push_back(&job);
+    while (!job.done) {
+        if (ctx->comb_busy) {
+            ctx->comb_cv.wait(lk);
+            continue;
+        }
+        ctx->comb_busy = true;
+        std::vector<OneshotJob *> take;
+        const int op = ctx->comb_q.front()->op, set = ctx->comb_q.front()->set;
+        size_t items = 0, bytes = 0;
+        for (auto it = ctx->comb_q.begin(); it != ctx->comb_q.end();) {
+            OneshotJob *q = *it;
+            const bool fits = take.empty() || (items + q->count <= kCombineItems && bytes + q->msg_bytes <= kCombineBytes);
+            if (q->op == op && q->set == set && fits) {
+                take.push_back(q);
+                items += q->count;
+                bytes += q->msg_bytes;
+                it = ctx->comb_q.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        lk.unlock();
+        const int rc = oneshot_run(ctx, op, set, take);
+        lk.lock();
+        for (OneshotJob *q : take) {
+            q->rc = rc;
+            q->done = true;   // its owner may return (and free it) once the lock is released
+        }
+        ctx->comb_busy = false;
+        ctx->comb_cv.notify_all();
+    }
+    return job.rc;
+}
+
+extern "C" {
 
 int cuspx_keypair_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *seeds, uint8_t *pks, uint8_t *sks) {
     if (!ctx || set < 0 || set >= kNumSets) return CUSPX_EINVAL;
     if (count == 0) return CUSPX_OK;
     if (!seeds || !pks || !sks) return fail(ctx, CUSPX_EINVAL, "keypair_batch: null buffer");
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cuspx_batch *b;
-    int rc = oneshot_batch(ctx, CUSPX_OP_KEYGEN, set, count, 0, &b);
-    if (rc) return rc;
-    const SetParams &P = b->P;
-    const size_t seed_b = count * 3 * P.n, sk_b = count * P.sk_bytes, pk_b = count * P.pk_bytes;
-    Staging st;
-    if ((rc = oneshot_stage(ctx, al16(seed_b) + al16(sk_b) + al16(pk_b), st))) return rc;
-    uint8_t *h_seed = (uint8_t *)st.take(seed_b);
-    uint8_t *h_sk = (uint8_t *)st.take(sk_b);
-    uint8_t *h_pk = (uint8_t *)st.take(pk_b);
-    memcpy(h_seed, seeds, seed_b);
-    if ((rc = cuspx_batch_upload(b, count, h_seed, count, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr)))
-        return rc;
-    if ((rc = cuspx_batch_run(b))) return rc;
-    if ((rc = cuspx_batch_download(b, h_sk, h_pk, nullptr))) return rc;
-    memcpy(sks, h_sk, sk_b);
-    memcpy(pks, h_pk, pk_b);
-    return CUSPX_OK;
+    OneshotJob j;
+    j.op = CUSPX_OP_KEYGEN;
+    j.set = set;
+    j.count = count;
+    j.keys = seeds;
+    j.out = pks;
+    j.out2 = sks;
+    return oneshot_submit(ctx, j);
 }
 
 int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, const uint8_t *msgs,
@@ -900,33 +1242,19 @@ int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, 
     if (!sks || !msg_off || !msg_len || !sigs) return fail(ctx, CUSPX_EINVAL, "sign_batch: null buffer");
     const size_t total = packed_bytes(count, msg_len);
     if (!msgs && total) return fail(ctx, CUSPX_EINVAL, "sign_batch: msgs is null but a message is not empty");
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cuspx_batch *b;
-    int rc = oneshot_batch(ctx, CUSPX_OP_SIGN, set, count, total, &b);
-    if (rc) return rc;
-    const SetParams &P = b->P;
-    const size_t sk_b = count * P.sk_bytes, opt_b = optrand ? count * P.n : 0, sig_b = count * P.sig_bytes;
-    Staging st;
-    if ((rc = oneshot_stage(ctx, al16(sk_b) + 2 * al16(count * 8) + al16(opt_b) + al16(total + 16) + al16(sig_b) +
-                                     al16(count * 4), st)))
-        return rc;
-    uint8_t *h_sk = (uint8_t *)st.take(sk_b);
-    uint64_t *h_off = (uint64_t *)st.take(count * 8);
-    uint64_t *h_len = (uint64_t *)st.take(count * 8);
-    uint8_t *h_opt = optrand ? (uint8_t *)st.take(opt_b) : nullptr;
-    uint8_t *h_msg = (uint8_t *)st.take(total + 16);
-    uint8_t *h_sig = (uint8_t *)st.take(sig_b);
-    int32_t *h_st = (int32_t *)st.take(count * 4);
-    memcpy(h_sk, sks, sk_b);
-    if (optrand) memcpy(h_opt, optrand, opt_b);
-    pack_staged(count, msgs, msg_off, msg_len, total, h_msg, h_off, h_len);
-    if ((rc = cuspx_batch_upload(b, count, h_sk, count, nullptr, h_msg, total, h_off, h_len, h_opt, nullptr)))
-        return rc;
-    if ((rc = cuspx_batch_run(b))) return rc;
-    if ((rc = cuspx_batch_download(b, h_sig, nullptr, h_st))) return rc;
-    memcpy(sigs, h_sig, sig_b);
-    if (status) memcpy(status, h_st, count * 4);
-    return CUSPX_OK;
+    OneshotJob j;
+    j.op = CUSPX_OP_SIGN;
+    j.set = set;
+    j.count = count;
+    j.keys = sks;
+    j.msgs = msgs;
+    j.off = msg_off;
+    j.len = msg_len;
+    j.aux = optrand;
+    j.out = sigs;
+    j.status = status;
+    j.msg_bytes = total;
+    return oneshot_submit(ctx, j);
 }
 
 int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks, const uint8_t *msgs,
@@ -937,33 +1265,19 @@ int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks
     if (!pks || !msg_off || !msg_len || !sigs || !verdicts) return fail(ctx, CUSPX_EINVAL, "verify_batch: null buffer");
     const size_t total = packed_bytes(count, msg_len);
     if (!msgs && total) return fail(ctx, CUSPX_EINVAL, "verify_batch: msgs is null but a message is not empty");
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cuspx_batch *b;
-    int rc = oneshot_batch(ctx, CUSPX_OP_VERIFY, set, count, total, &b);
-    if (rc) return rc;
-    const SetParams &P = b->P;
-    const size_t pk_b = count * P.pk_bytes, sig_b = count * P.sig_bytes, sl_b = siglens ? count * 8 : 0;
-    Staging st;
-    if ((rc = oneshot_stage(ctx, al16(pk_b) + 2 * al16(count * 8) + al16(sl_b) + al16(sig_b) + al16(total + 16) +
-                                     al16(count * 4), st)))
-        return rc;
-    uint8_t *h_pk = (uint8_t *)st.take(pk_b);
-    uint64_t *h_off = (uint64_t *)st.take(count * 8);
-    uint64_t *h_len = (uint64_t *)st.take(count * 8);
-    uint64_t *h_sl = siglens ? (uint64_t *)st.take(sl_b) : nullptr;
-    uint8_t *h_sig = (uint8_t *)st.take(sig_b);
-    uint8_t *h_msg = (uint8_t *)st.take(total + 16);
-    int32_t *h_v = (int32_t *)st.take(count * 4);
-    memcpy(h_pk, pks, pk_b);
-    if (siglens) memcpy(h_sl, siglens, sl_b);
-    memcpy(h_sig, sigs, sig_b);
-    pack_staged(count, msgs, msg_off, msg_len, total, h_msg, h_off, h_len);
-    if ((rc = cuspx_batch_upload(b, count, h_pk, count, nullptr, h_msg, total, h_off, h_len, h_sig, h_sl)))
-        return rc;
-    if ((rc = cuspx_batch_run(b))) return rc;
-    if ((rc = cuspx_batch_download(b, nullptr, nullptr, h_v))) return rc;
-    memcpy(verdicts, h_v, count * 4);
-    return CUSPX_OK;
+    OneshotJob j;
+    j.op = CUSPX_OP_VERIFY;
+    j.set = set;
+    j.count = count;
+    j.keys = pks;
+    j.msgs = msgs;
+    j.off = msg_off;
+    j.len = msg_len;
+    j.aux = sigs;
+    j.siglens = siglens;
+    j.status = verdicts;
+    j.msg_bytes = total;
+    return oneshot_submit(ctx, j);
 }
 
 // ---------------------------------------------------------------------------
@@ -986,7 +1300,7 @@ int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *
         for (int i = 0; i < nb && same; i++) {
             cuspx_batch *b = batches[i];
             same = g.batches[i] == b && g.counts[i] == b->count && g.long_msgs[i] == b->long_msgs &&
-                   memcmp(&g.tunes[i], &ctx->tune[b->set], sizeof(Tuning)) == 0;
+                   memcmp(&g.tunes[i], &effective_tuning(ctx, b->set, b->op, b->count), sizeof(Tuning)) == 0;
         }
         if (same) hit = &g;
     }
@@ -996,7 +1310,7 @@ int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *
         for (int i = 0; i < nb; i++) {
             gg.counts.push_back(batches[i]->count);
             gg.long_msgs.push_back(batches[i]->long_msgs);
-            gg.tunes.push_back(ctx->tune[batches[i]->set]);
+            gg.tunes.push_back(effective_tuning(ctx, batches[i]->set, batches[i]->op, batches[i]->count));
         }
         CK(cudaStreamCreateWithFlags(&gg.origin, cudaStreamNonBlocking), ctx);
         cudaEventCreate(&gg.e0);

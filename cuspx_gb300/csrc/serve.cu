@@ -32,7 +32,8 @@
 
 namespace cuspx {
 SetParams make_params(const SetDesc &s);
-int batch_set_stream_priority(cuspx_batch *b, int priority);
+int batch_share_stream(cuspx_batch *b, cudaStream_t s);
+void batch_use_stream(cuspx_batch *b, cudaStream_t s);
 void batch_direct_launch(cuspx_batch *b, bool on);
 }
 using namespace cuspx;
@@ -76,6 +77,7 @@ struct Slot {
     int32_t *h_status = nullptr;
     cudaEvent_t ev = nullptr;
     cudaEvent_t ev_start = nullptr, ev_end = nullptr;   // device time of the launch
+    int stream = -1;   // index in the class's pool of the current launch's stream
     bool busy = false;
     size_t bytes = 0;
     std::vector<Req *> reqs;
@@ -98,6 +100,19 @@ constexpr size_t kMidLaunchBytes = (size_t)32 << 20;
 constexpr size_t kLongLaunchBytes = (size_t)64 << 20;
 // a long-class launch holds at most 64 MiB / 128 KiB messages
 constexpr size_t kLongItems = kLongLaunchBytes / kMidMsg;
+// Streams per length class.  Each launch runs on the stream of its class's
+// pool with the fewest launches in flight.  The device has a fixed number of
+// hardware work queues (32 requested, see cuspx_create); with one stream per
+// slot -- 2 operations x sets x classes x slots of them -- streams outnumber
+// the queues and a short launch could wait in a queue behind a 1 MiB
+// message-hashing kernel of another class (measured: <= 1 KiB sign p99 of
+// 95 ms at 20k req/s of the mixed 16 B..1 MiB stream, 8.8 ms with pools).
+// The long class gets the most streams: its launches last ~33-46 ms (serial
+// hashing of a 1 MiB message) while using few SMs, so many must overlap.
+constexpr int kClassStreams[kClasses] = {8, 8, 16};
+// launch slots per group: max_inflight, and at least kLongSlots for long
+// messages (whose launches are long but light)
+constexpr int kLongSlots = 6;
 
 int class_of(size_t mlen) { return mlen <= kShortMsg ? 0 : (mlen <= kMidMsg ? 1 : 2); }
 
@@ -173,6 +188,8 @@ struct cuspx_server {
     double launch_ms_sum = 0, launch_ms_max = 0;
     LatHist lat_sign, lat_verify;
     LatHist lat_bucket[2][3];   // [sign, verify][<= 1 KiB, <= 64 KiB, > 64 KiB]
+    std::vector<cudaStream_t> streams[kClasses];   // per-class stream pools
+    std::vector<int> stream_load[kClasses];         // launches in flight per pooled stream (under mu)
     uint64_t done_by_set[2][kNumSets] = {};   // [sign, verify][set]
     double msg_units_by_set[kNumSets] = {};
     Clock::time_point last_done;
@@ -214,6 +231,9 @@ static size_t class_msg_bytes(const cuspx_server *s, const Group &g) {
 static size_t class_items(const cuspx_server *s, const Group &g) {
     return g.cls == 2 ? std::min<size_t>(s->cfg.max_batch, kLongItems) : (size_t)s->cfg.max_batch;
 }
+static int class_slots(const cuspx_server *s, const Group &g) {
+    return g.cls == 2 ? std::max(s->cfg.max_inflight, kLongSlots) : s->cfg.max_inflight;
+}
 
 // Create a slot's batch and pinned staging once, at the full size of its
 // group (the class's items and message area).
@@ -224,11 +244,7 @@ static bool size_slot(cuspx_server *s, Group &g, Slot *sl) {
     const size_t msg_cap = class_msg_bytes(s, g);
     if (cuspx_batch_create(s->ctx, g.op, g.set, cap, msg_cap, 1, &sl->b) != CUSPX_OK) return false;
     batch_direct_launch(sl->b, true);   // no graph instantiation while serving
-    // short-message launches run ahead of middle ones, those ahead of long
-    // ones on the GPU (lo is the least urgent priority, hi the most)
-    int lo = 0, hi = 0;
-    cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    batch_set_stream_priority(sl->b, g.cls == 0 ? hi : (g.cls == 1 ? (lo + hi) / 2 : lo));
+    batch_share_stream(sl->b, s->streams[g.cls][0]);   // the launch picks its stream
     const KeyTable &kt = s->keys[g.set];
     cuspx_batch_bind_keys(sl->b, g.op == CUSPX_OP_SIGN ? kt.d_sk : kt.d_pk, kt.cap);
     auto host = [](void **p, size_t bytes) { return cudaMallocHost(p, std::max<size_t>(bytes, 16)) == cudaSuccess; };
@@ -250,7 +266,10 @@ static bool size_slot(cuspx_server *s, Group &g, Slot *sl) {
 static bool launch_slot(cuspx_server *s, Group &g, Slot *sl) {
     const SetParams &P = g.P;
     if (!size_slot(s, g, sl)) return false;
-    cudaStream_t st = (cudaStream_t)cuspx_batch_stream(sl->b);
+    // the slot is idle (its last launch completed): move it to the stream
+    // chosen for this launch without waiting for anything
+    cudaStream_t st = s->streams[g.cls][sl->stream];
+    batch_use_stream(sl->b, st);
     cudaEventRecord(sl->ev_start, st);
     size_t off = 0;
     for (size_t i = 0; i < sl->reqs.size(); i++) {
@@ -321,6 +340,8 @@ static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
     }
     s->last_done = now;
     sl->reqs.clear();
+    if (sl->stream >= 0) s->stream_load[g.cls][sl->stream]--;
+    sl->stream = -1;
     s->bytes_inflight -= sl->bytes;
     sl->bytes = 0;
     sl->busy = false;
@@ -375,7 +396,7 @@ static void scheduler(cuspx_server *s, int lc) {
                     break;
                 }
                 if (!free_sl) {
-                    if ((int)g.slots.size() >= s->cfg.max_inflight) break;
+                    if ((int)g.slots.size() >= class_slots(s, g)) break;
                     free_sl = new Slot();
                     g.slots.push_back(free_sl);
                 }
@@ -401,6 +422,15 @@ static void scheduler(cuspx_server *s, int lc) {
                 s->pending_bytes -= bytes;
                 free_sl->busy = true;
                 free_sl->bytes = bytes;
+                {
+                    // the class's least loaded stream
+                    std::vector<int> &load = s->stream_load[g.cls];
+                    int best = 0;
+                    for (int i = 1; i < (int)load.size(); i++)
+                        if (load[i] < load[best]) best = i;
+                    load[best]++;
+                    free_sl->stream = best;
+                }
                 s->bytes_inflight += bytes;
                 s->bytes_peak = std::max(s->bytes_peak, s->bytes_inflight);
                 s->launches++;
@@ -444,6 +474,24 @@ int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_serv
                 g.P = make_params(kSets[set]);
                 g.per_item = item_bytes(op, g.P);
             }
+    // short-message launches run ahead of middle ones, those ahead of long
+    // ones on the GPU (lo is the least urgent priority, hi the most)
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    for (int lc = 0; lc < kClasses; lc++) {
+        const int prio = lc == 0 ? hi : (lc == 1 ? (lo + hi) / 2 : lo);
+        for (int i = 0; i < kClassStreams[lc]; i++) {
+            cudaStream_t st = nullptr;
+            if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio) != cudaSuccess) {
+                for (auto &p : s->streams)
+                    for (cudaStream_t x : p) cudaStreamDestroy(x);
+                delete s;
+                return CUSPX_ECUDA;
+            }
+            s->streams[lc].push_back(st);
+        }
+        s->stream_load[lc].assign(s->streams[lc].size(), 0);
+    }
     for (int lc = 0; lc < kClasses; lc++) s->th[lc] = std::thread(scheduler, s, lc);
     *out = s;
     return CUSPX_OK;
@@ -471,6 +519,8 @@ void cuspx_serve_destroy(cuspx_server *s) {
         cudaFree(kt.d_sk);
         cudaFree(kt.d_pk);
     }
+    for (auto &p : s->streams)
+        for (cudaStream_t x : p) cudaStreamDestroy(x);
     delete s;
 }
 
@@ -522,7 +572,7 @@ int cuspx_serve_prepare(cuspx_server *s, int op, int set) {
     if (int rc = ensure_table(s, set)) return rc;
     for (int lc = 0; lc < kClasses; lc++) {
         Group &g = s->group(op, set, lc);
-        while ((int)g.slots.size() < s->cfg.max_inflight) {
+        while ((int)g.slots.size() < class_slots(s, g)) {
             Slot *sl = new Slot();
             if (!size_slot(s, g, sl)) {
                 free_slot(sl);

@@ -26,6 +26,7 @@ struct Tuning {
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
     int verify_slots = 4;    // most items per warp in the persistent verify kernel
+    int verify_item_max = 0; // batches of at most this many items verify one item per block
 };
 
 struct KeygenArgs {
@@ -133,6 +134,7 @@ struct Family {
         if constexpr (kPersistVerify)
             if ((e = cudaFuncSetAttribute(k_verify_hyper<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big)))
                 return e;
+        if ((e = cudaFuncSetAttribute(k_verify_item<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         // Load every other kernel of the family now: with lazy module loading
         // a kernel's first launch loads it, and in a server that first launch
         // is a request's (one took ~50 ms of host time and held back every
@@ -275,6 +277,14 @@ struct Family {
         }
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
         CUSPX_MARK(pt, "k_verify_fors", s);
+        if (tu.verify_item_max > 0 && A.count <= (uint32_t)tu.verify_item_max && P.hp <= 9) {
+            // small batches: one item per block (its serial path sets the time)
+            constexpr int LEN = 2 * N + 3, CW = (LEN + 31) / 32;
+            const size_t smem = (size_t)VerifyPolicy<HF>::slot_words(P.hp) * 4;
+            k_verify_item<HF><<<A.count, 32 * (CW + 1), smem, s>>>(P, A);
+            CUSPX_MARK(pt, "k_verify_item", s);
+            return;
+        }
         const int b = tu.verify_block;
         if (tu.verify_mode == 2 && kPersistVerify && A.ctr && P.hp <= 9) {
             verify_persistent(P, A, tu, s, pt);

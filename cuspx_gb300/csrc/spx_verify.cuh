@@ -1092,4 +1092,219 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Per-item verify for small batches (crypto_sign_verify, sign.cu:3048-3121).
+//
+// A lone item is bound by its serial path: per layer the longest WOTS+ chain
+// (up to 15 F), the T_len blocks after it and h' H.  Here one block holds
+// one item in a single slot of the persistent kernel's layout: thread c of
+// the ceil(len / 32) chain warps runs chain c of every layer with the chain
+// step precompute (f_prepare / f_step: rounds 0-4 of each SHA-256 F are
+// shared by the whole chain), writes the chain end into the slot's T stream
+// and sets its done bit; lane 0 of the last warp (the T warp) absorbs each
+// T block as soon as the chains it covers are done, then climbs the auth
+// path, and the T warp frames the next layer's stream.  One __syncthreads
+// per layer hands the root to the chain threads.  The chain threads never
+// wait; the T lane's wait for done bits is bounded (kItemSpinLimit polls,
+// each after a short sleep): if it ever ran out the item's verdict is -3
+// and the layer loop ends at once.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kItemSpinLimit = 1u << 22;
+
+template <class HF>
+__global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) {
+    using PV = VerifyPolicy<HF>;
+    constexpr int W = PV::W, N = PV::N, LEN = PV::LEN;
+    constexpr int CW = (LEN + 31) / 32;   // chain warps; warp CW is the T warp
+    extern __shared__ uint32_t smem[];
+    __shared__ int s_fail;
+    uint32_t *S = smem;
+    uint32_t *stream = S + PV::S_HDR;
+    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    const bool tw = (tid >> 5) == (uint32_t)CW;
+    const uint32_t it = blockIdx.x;
+    if (it >= A.count) return;   // uniform over the block
+    const SignWork *wk = A.work + it;
+    if (wk->flags) {   // wrong signature length (sign.cu:3063-3065)
+        if (tid == 0) A.verdict[it] = -1;
+        return;
+    }
+    const uint64_t tree = wk->tree;
+    const uint32_t idx_leaf = wk->idx_leaf;
+    const uint8_t *pk = A.pk.row(it);
+    const uint8_t *sig = A.sig + (uint64_t)it * A.sig_stride + N + P.fors_bytes;
+    typename PV::LaneRegs lr{};
+
+    // T warp: frame the stream of layer L (ADRS, padding, no value present)
+    auto frame_layer = [&](int L) {
+        uint64_t tree_L;
+        uint32_t idx_L;
+        layer_index(P, tree, idx_leaf, L, tree_L, idx_L);
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_layer(pa, L);
+        adrs_tree(pa, tree_L);
+        adrs_keypair(pa, idx_L);
+        adrs_type(pa, ADDR_WOTSPK);
+        PV::frame(stream, S, pa, LEN, lane);
+        if (lane == 0) {
+            Adrs wa;
+            adrs_zero(wa);
+            adrs_layer(wa, L);
+            adrs_tree(wa, tree_L);
+            adrs_type(wa, ADDR_WOTS);
+            adrs_keypair(wa, idx_L);
+            S[PV::S_AW0] = wa.w[0];
+            S[PV::S_AW1] = wa.w[1];
+            S[PV::S_AW2] = wa.w[2];
+            S[PV::S_IDXL] = idx_L;
+            S[PV::S_LAYER] = (uint32_t)L;
+            S[PV::S_M] = LEN;
+            S[PV::S_NB] = PV::stream_blocks(LEN);
+            S[PV::S_MASK] = PV::mask_init(0, LEN);
+            S[PV::S_MASK + 1] = PV::mask_init(1, LEN);
+            S[PV::S_MASK + 2] = PV::mask_init(2, LEN);
+        }
+        // the auth path of layer L
+        uint32_t *auth = stream + PV::kStreamWords;
+        const uint8_t *sl = sig + (uint64_t)L * (P.wots_bytes + P.hp * N);
+        for (int q = lane; q < P.hp * W; q += 32) auth[q] = reinterpret_cast<const uint32_t *>(sl + P.wots_bytes)[q];
+    };
+    // T lane: absorb the slot's stream block by block as its values arrive;
+    // false if the wait ran out
+    auto run_t = [&](uint32_t out[W]) -> bool {
+        PV::claim_t(lr, S, P.hp);
+        const int nb = (int)S[PV::S_NB];
+        const int m = (int)S[PV::S_M];
+        uint32_t spins = 0;
+        for (int j = 0; j < nb;) {
+            int act;
+            if constexpr (PV::kTMask) act = PV::t_action(S, j);
+            else act = PV::done_prefix(S) > PV::block_last_value(j, m) ? 0 : 2;
+            if (act == 2) {
+                if (++spins > kItemSpinLimit) return false;
+                __nanosleep(64);
+                __threadfence_block();   // re-read the done bits; order the value reads after them
+                continue;
+            }
+            __threadfence_block();
+            typename PV::Unit u;
+            if constexpr (PV::kTMask) {
+                if (act == 1) {
+                    PV::build_mask(u, S, P.hp);
+                    PV::run(u);
+                    PV::after_mask(u, S, P.hp);
+                    continue;
+                }
+            }
+            PV::build_t(u, lr, S, j, P.hp);
+            PV::run(u);
+            PV::after_t(u, lr, S, P.hp);
+            if (++j == nb) PV::value_out(u, out);
+        }
+        return true;
+    };
+    // T lane: root of the current layer's tree from its leaf
+    auto climb = [&](uint32_t v[W]) {
+        uint32_t idx = S[PV::S_IDXL];
+        for (int h = 0; h < P.hp; h++) {
+            for (int sub = 0; sub < PV::kHUnits; sub++) {
+                typename PV::Unit u;
+                PV::build_h(u, lr, S, h, sub, idx, v, P.hp);
+                PV::run(u);
+                if (sub < PV::kHUnits - 1) PV::after_h_unit(u, lr, sub);
+                else PV::value_out(u, v);
+            }
+            idx >>= 1;
+        }
+    };
+
+    if (tid == 0) s_fail = 0;
+    // ---- T_k over the FORS roots (fors.cu:141-142): the message of layer 0 ----
+    if (tw) {
+        PV::load_key(S, wk, pk, lane);
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_tree(pa, tree);
+        adrs_keypair(pa, idx_leaf);
+        adrs_type(pa, ADDR_FORSPK);
+        __syncwarp();
+        PV::frame(stream, S, pa, P.k, lane);
+        PV::copy_values(stream, A.fors_roots + (uint64_t)it * P.k * N, P.k * N, lane);
+        if (lane == 0) {
+            S[PV::S_LAYER] = (uint32_t)-1;
+            S[PV::S_M] = P.k;
+            S[PV::S_NB] = PV::stream_blocks(P.k);
+            S[PV::S_MASK] = S[PV::S_MASK + 1] = S[PV::S_MASK + 2] = ~0u;   // every value present
+        }
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t root[W];
+            if (!run_t(root)) s_fail = 1;
+#pragma unroll
+            for (int i = 0; i < W; i++) S[PV::S_ROOT + i] = root[i];
+        }
+        __syncwarp();
+        frame_layer(0);
+    }
+    __syncthreads();
+
+    // ---- the d layers (wots_pk_from_sig + T_len + compute_root each) ----
+    KeyRegs<N> key;
+    if (!tw && tid < LEN) key_from_work<HF>(key, pk, pk, *wk);
+    for (int L = 0; L < P.d && !s_fail; L++) {
+        if (!tw) {
+            if (tid < LEN) {
+                const int c = (int)tid;
+                uint32_t root[W], v[W];
+#pragma unroll
+                for (int i = 0; i < W; i++) root[i] = S[PV::S_ROOT + i];
+                const uint32_t ln = chain_len<HF>(P, root, c);
+                HF::load(v, sig + (uint64_t)L * (P.wots_bytes + P.hp * N) + (uint64_t)c * N);
+                if (ln < 15) {
+                    uint64_t tree_L;
+                    uint32_t idx_L;
+                    layer_index(P, tree, idx_leaf, L, tree_L, idx_L);
+                    Adrs wa;
+                    adrs_zero(wa);
+                    adrs_layer(wa, L);
+                    adrs_tree(wa, tree_L);
+                    adrs_type(wa, ADDR_WOTS);
+                    adrs_keypair(wa, idx_L);
+                    adrs_chain(wa, c);
+                    typename HF::FCtx fc;
+                    HF::f_prepare(fc, wa, key);
+                    for (uint32_t s = ln; s < 15; s++) HF::f_step(v, v, fc, s, key);
+                }
+                PV::write_value(stream, c, v);
+                __threadfence_block();   // the value before its done bit
+                PV::mark_done(S, c);
+            }
+        } else {
+            if (lane == 0) {
+                uint32_t v[W];
+                if (!run_t(v)) {
+                    s_fail = 1;
+                } else {
+                    climb(v);
+                    if (L == P.d - 1) {
+                        uint32_t pr[W];
+                        HF::load(pr, pk + N);
+                        bool ok = true;
+#pragma unroll
+                        for (int i = 0; i < W; i++) ok &= pr[i] == v[i];
+                        A.verdict[it] = ok ? 0 : -1;
+                    }
+#pragma unroll
+                    for (int i = 0; i < W; i++) S[PV::S_ROOT + i] = v[i];
+                }
+            }
+            __syncwarp();
+            if (L + 1 < P.d && !s_fail) frame_layer(L + 1);
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && s_fail) A.verdict[it] = -3;   // a T wait ran out (never expected)
+}
+
 }  // namespace cuspx

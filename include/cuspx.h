@@ -77,11 +77,38 @@ typedef struct {
                              unless this is 0 */
     int verify_slots;     /* most items a warp holds at once in verify_mode 2 (1..8); batches
                              below about 4 warps per SM use fewer */
+    int verify_item_max;  /* verify batches of at most this many items (any verify_mode) with one
+                             thread block per item: a thread per WOTS+ chain and a T lane that
+                             streams T_len behind the chains (0: never) */
 } cuspx_tuning;
 /* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2,
- * tree_mode and chain_mode_max, which keep it when < 0 */
+ * tree_mode, chain_mode_max and verify_item_max, which keep it when < 0 */
 int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
 int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
+/* Mappings by batch size (what the autotuner installs): the mapping of
+ * `set` for `op` batches of at most max_count items, built from the set's
+ * current base mapping with t's fields applied (cuspx_set_tuning's rules).
+ * A batch of `count` items runs with the entry of smallest max_count >=
+ * count (the largest entry for bigger batches), or with the base mapping
+ * when (set, op) has no entry.  Entries take precedence over the base;
+ * at most 16 per (set, op).  Change mappings while no batch of the set is
+ * being launched. */
+int cuspx_set_tuning_for(cuspx_ctx *ctx, int set, int op, size_t max_count, const cuspx_tuning *t);
+/* the mapping a batch of `count` items of (set, op) runs with */
+int cuspx_get_tuning_for(cuspx_ctx *ctx, int set, int op, size_t count, cuspx_tuning *t);
+/* drop the entries of (set, op), or of every op when op < 0 */
+int cuspx_clear_tuning_for(cuspx_ctx *ctx, int set, int op);
+/* Install the entries of a tuning file written by the autotuner
+ * (cuspx_gb300/autotune.py): one tab-separated line per entry,
+ *   <gpu name> <set name> <sign|verify|keygen> <max_count> <ms> <knob>=<v>,...
+ * Lines of other GPUs are skipped.  cuspx_create reads $CUSPX_TUNE_CACHE
+ * (default $HOME/.cache/cuspx/tune.tsv) when it exists, so the api.h
+ * drop-ins, the one-shot calls and serving all run the tuned mappings.
+ * Returns the number of entries installed, or a negative error.  Replaces
+ * the reference's compile-time launch knobs (all_option.h:7-68). */
+int cuspx_load_tuning(cuspx_ctx *ctx, const char *path);
+/* the CUDA device name (as the tuning file records it) */
+int cuspx_device_name(int device, char *buf, size_t len);
 
 /* ---- one-shot calls on host buffers (synchronous) ----------------------- */
 /* seeds: count x 3n; writes pks: count x 2n, sks: count x 4n
@@ -96,7 +123,9 @@ int cuspx_sign_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *sks, 
                      int32_t *status);
 /* pks: count x 2n rows; sigs: count rows of sig_bytes; siglens: per item
  * (NULL = sig_bytes).  verdicts[i] = 0 accept, -1 reject
- * (crypto_sign_verify, sign.cu:3048-3121). */
+ * (crypto_sign_verify, sign.cu:3048-3121); -3 if the per-item verify kernel
+ * (cuspx_tuning.verify_item_max) gave up waiting for its own chain threads,
+ * which its design never lets happen (the wait is bounded all the same). */
 int cuspx_verify_batch(cuspx_ctx *ctx, int set, size_t count, const uint8_t *pks, const uint8_t *msgs,
                        const uint64_t *msg_off, const uint64_t *msg_len, const uint8_t *sigs,
                        const uint64_t *siglens, int32_t *verdicts);
@@ -197,6 +226,12 @@ int cuspx_sign_noalloc(int set, size_t count, const uint8_t *d_sks, const uint8_
  * reference, which publishes no roofline. */
 int cuspx_int_peak_mix(int device, int iters, int mix, double *ops_per_s, float *ms);
 int cuspx_int_peak(int device, int iters, double *ops_per_s, float *ms);
+/* SHA-256 compressions per second over all SMs, with warps_per_sm warps on
+ * every SM, each lane running `iters` compressions in a dependent chain (each
+ * block built from the previous state); *ns_per_cmp (may be NULL) is the
+ * time of one compression in such a chain.  At one warp per SM this is the
+ * compression's latency, the floor of a serial hash path. */
+int cuspx_cmp_rate(int device, int warps_per_sm, int iters, double *cmp_per_s, double *ns_per_cmp);
 
 #ifdef __cplusplus
 }

@@ -103,10 +103,20 @@ static inline void put_be32(uint8_t *p, uint32_t v)
     p[0] = (uint8_t)(v >> 24); p[1] = (uint8_t)(v >> 16); p[2] = (uint8_t)(v >> 8); p[3] = (uint8_t)v;
 }
 
+/* Hash-unit counters of the calling thread: [0] SHA-256 compressions,
+ * [1] Keccak-f[1600] permutations, [2] the units of both spent inside
+ * wots_sign (the reference recomputes the signing leaf's chains there).
+ * Test infrastructure: they pin the work model behind the benchmark's
+ * roofline fractions. */
+static _Thread_local unsigned long long g_units[3];
+void spxo_units(unsigned long long out[3]) { memcpy(out, g_units, sizeof g_units); }
+void spxo_units_reset(void) { memset(g_units, 0, sizeof g_units); }
+
 /* one 64-byte block (crypto_hashblocks_sha256, sha256.cu:103-259) */
 static void sha256_block(uint32_t s[8], const uint8_t *blk)
 {
     uint32_t w[64];
+    g_units[0]++;
     for (int i = 0; i < 16; i++) w[i] = be32(blk + 4 * i);
     for (int i = 16; i < 64; i++) {
         uint32_t s0 = rotr32(w[i - 15], 7) ^ rotr32(w[i - 15], 18) ^ (w[i - 15] >> 3);
@@ -216,6 +226,7 @@ static inline uint64_t rotl64(uint64_t v, int c) { return c ? (v << c) | (v >> (
 
 static void keccak_f1600(uint64_t s[25])
 {
+    g_units[1]++;
     for (int r = 0; r < 24; r++) {
         uint64_t C[5], D[5], B[25];
         for (int x = 0; x < 5; x++) C[x] = s[x] ^ s[x + 5] ^ s[x + 10] ^ s[x + 15] ^ s[x + 20];
@@ -515,6 +526,7 @@ static void wots_sign(const hctx *hc, uint8_t *sig, const uint8_t *msg, uint8_t 
 {
     const int n = hc->p->n;
     unsigned len[80];
+    const unsigned long long before = g_units[0] + g_units[1];
     chain_lengths(hc->p, len, msg);
     for (int i = 0; i < hc->p->len; i++) {
         set_chain(addr, i);
@@ -522,6 +534,7 @@ static void wots_sign(const hctx *hc, uint8_t *sig, const uint8_t *msg, uint8_t 
         prf_addr(hc, sig + i * n, addr);
         gen_chain(hc, sig + i * n, sig + i * n, 0, len[i], addr);
     }
+    g_units[2] += g_units[0] + g_units[1] - before;
 }
 
 /* wots_pk_from_sig (wots.cu:777-789) */

@@ -91,6 +91,12 @@ void spxo_drbg_bytes(spxo_drbg *s, uint8_t *out, size_t len);
 void spxo_randombytes_init(const uint8_t entropy[48]);
 void spxo_randombytes(uint8_t *out, size_t len);
 
+/* Hash units counted on the calling thread since spxo_units_reset:
+ * out[0] SHA-256 compressions, out[1] Keccak-f[1600] permutations, out[2]
+ * the units of both inside wots_sign (wots.cu:614-625). */
+void spxo_units(unsigned long long out[3]);
+void spxo_units_reset(void);
+
 /* Bounded multi-threaded throughput probe used by the CPU baseline: each of
  * `threads` workers signs (op=0) or verifies (op=1) its share of `count`
  * items with distinct seeded keys for at least `min_seconds`.  Returns the

@@ -64,6 +64,10 @@ def lib():
         L.spxo_throughput.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_size_t, ctypes.c_double,
                                       ctypes.c_long, ctypes.POINTER(ctypes.c_double)]
         L.spxo_throughput.restype = ctypes.c_long
+        L.spxo_units.argtypes = [ctypes.POINTER(ctypes.c_ulonglong * 3)]
+        L.spxo_units.restype = None
+        L.spxo_units_reset.argtypes = []
+        L.spxo_units_reset.restype = None
         _lib = L
     return _lib
 
@@ -124,6 +128,18 @@ class Oracle:
         done = self.L.spxo_throughput(ctypes.byref(self.p), op, threads, mlen, seconds, max_ops,
                                       ctypes.byref(secs))
         return done, secs.value
+
+
+def units_reset():
+    lib().spxo_units_reset()
+
+
+def units():
+    """(SHA-256 compressions, Keccak-f permutations, units inside wots_sign)
+    counted on this thread since units_reset()."""
+    a = (ctypes.c_ulonglong * 3)()
+    lib().spxo_units(ctypes.byref(a))
+    return tuple(a)
 
 
 def sha256(data):

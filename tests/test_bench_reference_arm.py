@@ -29,6 +29,9 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "sign/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["set"] == "sha256-128f-simple" and d["config"]["batch"] == 4096
+    # a step is one measured 2-s sample, not an extrapolated batch time
+    assert 1500 < d["ms_per_step"] < 10000 and d["step"]
+    assert cb["cpu_model"]
 
 
 def test_reference_arm_other_ranks_are_silent():

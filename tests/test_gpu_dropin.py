@@ -180,3 +180,53 @@ def test_dropin_release_mode_matches_reference(setname):
         assert tail.raw.hex() == g["drbg_tail16"]
     finally:
         L.cuspx_set_deterministic(1)
+
+
+def test_dropin_concurrent_threads_share_launches():
+    """Eight threads call crypto_sign_signature and crypto_sign_verify of one
+    drop-in at once (the reference's CPU API is not thread-safe at all:
+    sha256.cu:385 keeps a global hash state).  Concurrent calls are combined
+    into shared launches; every signature equals the oracle's and every
+    verdict is right, corrupted signatures included."""
+    import threading
+    import spx_oracle
+    L = _lib("sha256-128f")
+    o = spx_oracle.Oracle("sha256-128f-simple")
+    sigb = L.crypto_sign_bytes()
+    pk = ctypes.create_string_buffer(32)
+    sk = ctypes.create_string_buffer(64)
+    assert L.crypto_sign_seed_keypair(pk, sk, bytes(range(100, 148))) == 0
+    pk_b, sk_b = pk.raw, sk.raw
+    nthreads, per = 8, 6
+    msgs = [[hashlib.sha256(b"%d/%d" % (t, i)).digest() * (1 + (t + i) % 5) for i in range(per)]
+            for t in range(nthreads)]
+    results = [[None] * per for _ in range(nthreads)]
+    verdicts = [[None] * per for _ in range(nthreads)]
+    errors = []
+    start = threading.Barrier(nthreads)
+
+    def worker(t):
+        try:
+            start.wait()
+            sig = ctypes.create_string_buffer(sigb)
+            sl = ctypes.c_size_t()
+            for i, m in enumerate(msgs[t]):
+                assert L.crypto_sign_signature(sig, ctypes.byref(sl), m, len(m), sk_b) == 0
+                results[t][i] = sig.raw
+                bad = bytearray(sig.raw)
+                bad[(t * 977 + i * 131) % sigb] ^= 0x20
+                verdicts[t][i] = (L.crypto_sign_verify(sig.raw, sigb, m, len(m), pk_b),
+                                  L.crypto_sign_verify(bytes(bad), sigb, m, len(m), pk_b))
+        except Exception as e:   # reported below
+            errors.append(repr(e))
+
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(nthreads)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    assert not errors, errors
+    for t in range(nthreads):
+        for i, m in enumerate(msgs[t]):
+            assert results[t][i] == o.sign(m, sk_b), (t, i)
+            assert verdicts[t][i] == (0, -1), (t, i)

@@ -161,16 +161,22 @@ def test_verify_mappings_agree(engine, setname):
                   {"verify_mode": 2, "verify_slots": 1, "verify_block": 32},
                   {"verify_mode": 2, "verify_slots": 3, "verify_block": 64},
                   {"verify_mode": 2, "verify_slots": 8, "verify_block": 128}):
-            engine.set_tuning(sid, **m)
+            engine.set_tuning(sid, verify_item_max=0, **m)
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
             assert list(got) == want, m
+        # one item per block (the small-batch kernel)
+        engine.set_tuning(sid, verify_item_max=64)
+        assert list(engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)) == want
         # a batch large enough that the persistent kernel packs several
-        # items into each warp (1300 items on 152 SMs: 3 per warp)
+        # items into each warp (1300 items on 152 SMs: 3 per warp), and the
+        # same batch one item per block (several blocks share each SM)
         rep = 1300
-        engine.set_tuning(sid, verify_mode=2, verify_slots=8, verify_block=64)
-        got = engine.verify_batch(sid, [pks[kidx[i % 12]] for i in range(rep)], [msgs[i % 12] for i in range(rep)],
-                                  [sigs[i % 12] for i in range(rep)])
-        assert list(got) == [want[i % 12] for i in range(rep)]
+        for m in ({"verify_mode": 2, "verify_slots": 8, "verify_block": 64, "verify_item_max": 0},
+                  {"verify_item_max": 2000}):
+            engine.set_tuning(sid, **m)
+            got = engine.verify_batch(sid, [pks[kidx[i % 12]] for i in range(rep)],
+                                      [msgs[i % 12] for i in range(rep)], [sigs[i % 12] for i in range(rep)])
+            assert list(got) == [want[i % 12] for i in range(rep)], m
     finally:
         engine.set_tuning(sid, **saved)
 
@@ -202,8 +208,8 @@ def test_persistent_verify_refills_slots(engine):
     pick = [rng.randrange(len(cases)) for _ in range(count)]
     saved = engine.get_tuning(sid)
     try:
-        for m in ({"verify_mode": 2, "verify_slots": 1, "verify_block": 32},
-                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 128}):
+        for m in ({"verify_mode": 2, "verify_slots": 1, "verify_block": 32, "verify_item_max": 0},
+                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 128, "verify_item_max": 0}):
             engine.set_tuning(sid, **m)
             got = engine.verify_batch(sid, [pk] * count, [cases[j][1] for j in pick], [cases[j][0] for j in pick],
                                       siglens=[cases[j][2] for j in pick])

@@ -1,0 +1,90 @@
+"""The autotuner's result lives in the library: tune() installs a per-size
+mapping in the engine, records it in the tuning file, and a new context
+(cuspx_create) reads that file, so every caller of the C ABI -- drop-ins,
+one-shot calls, serving -- runs the tuned mapping."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _verify_batch_ms(eng, c, sid, n, reps=5):
+    z = c.set_sizes(sid)
+    rng = np.random.default_rng(77)
+    pks, sks = eng.keypair_batch(sid, [rng.bytes(z["seed"])])
+    msgs = [rng.bytes(64) for _ in range(n)]
+    sigs, _ = eng.sign_batch(sid, [sks[0]] * n, msgs)
+    slab, offs, lens = c.pack_messages(msgs)
+    b = eng.batch(c.OP_VERIFY, sid, n, len(slab), 1)
+    b.upload(n, pks[0], 1, np.zeros(n, dtype=np.uint32), slab, len(slab), offs, lens,
+             np.frombuffer(b"".join(sigs), dtype=np.uint8))
+    best = None
+    for _ in range(reps):
+        b.run()
+        b.sync()
+        best = b.last_ms() if best is None else min(best, b.last_ms())
+    v = np.zeros(n, dtype=np.int32)
+    b.download(None, None, v)
+    b.close()
+    assert (v == 0).all()
+    return best
+
+
+def test_tune_is_installed_in_the_library_and_round_trips(tmp_path, monkeypatch):
+    import cuspx_gb300 as c
+    from cuspx_gb300 import autotune
+    path = tmp_path / "tune.tsv"
+    monkeypatch.setenv("CUSPX_TUNE_CACHE", str(path))
+    eng = c.Engine(0)
+    try:
+        sid = c.set_id("sha256-128f-simple")
+        n = 256
+        default_ms = _verify_batch_ms(eng, c, sid, n)
+        mapping, best = autotune.tune(eng, sid, c.OP_VERIFY, count=n, reps=2, passes=1)
+        # the engine runs the tuned mapping for this size, the base is untouched
+        got = eng.get_tuning_for(sid, c.OP_VERIFY, n)
+        assert {k: got[k] for k in mapping} == mapping
+        tuned_ms = _verify_batch_ms(eng, c, sid, n)
+        assert tuned_ms <= default_ms * 1.15, (tuned_ms, default_ms, mapping)
+        assert path.exists()
+        assert autotune.load_cache(str(path))[(c.device_name(), "sha256-128f-simple", "verify", 256)][1] == mapping
+    finally:
+        eng.close()
+    # a new context reads the file at creation
+    eng2 = c.Engine(0)
+    try:
+        got = eng2.get_tuning_for(sid, c.OP_VERIFY, n)
+        assert {k: got[k] for k in mapping} == mapping
+        # sizes above the largest entry take it too; other ops and sets keep their base
+        assert {k: eng2.get_tuning_for(sid, c.OP_VERIFY, 5000)[k] for k in mapping} == mapping
+        assert eng2.get_tuning_for(sid, c.OP_SIGN, n) == eng2.get_tuning(sid)
+        eng2.clear_tuning_for(sid)
+        assert eng2.get_tuning_for(sid, c.OP_VERIFY, n) == eng2.get_tuning(sid)
+        assert eng2.load_tuning(str(path)) == 1
+    finally:
+        eng2.close()
+
+
+def test_per_size_entries_pick_the_smallest_cover(monkeypatch, tmp_path):
+    import cuspx_gb300 as c
+    monkeypatch.setenv("CUSPX_TUNE_CACHE", str(tmp_path / "none.tsv"))
+    eng = c.Engine(0)
+    try:
+        sid = c.set_id("shake256-128f-simple")
+        eng.set_tuning_for(sid, c.OP_SIGN, 64, leaf_block=64)
+        eng.set_tuning_for(sid, c.OP_SIGN, 1024, leaf_block=256)
+        assert eng.get_tuning_for(sid, c.OP_SIGN, 1)["leaf_block"] == 64
+        assert eng.get_tuning_for(sid, c.OP_SIGN, 64)["leaf_block"] == 64
+        assert eng.get_tuning_for(sid, c.OP_SIGN, 65)["leaf_block"] == 256
+        assert eng.get_tuning_for(sid, c.OP_SIGN, 99999)["leaf_block"] == 256
+        # every entry gives the oracle's bytes
+        import spx_oracle
+        o = spx_oracle.Oracle("shake256-128f-simple")
+        pk, sk = o.seed_keypair(bytes(range(48)))
+        for count in (3, 70):
+            msgs = [bytes([i]) * (i + 1) for i in range(count)]
+            sigs, st = eng.sign_batch(sid, [sk] * count, msgs)
+            assert list(st) == [0] * count
+            assert sigs[0] == o.sign(msgs[0], sk) and sigs[-1] == o.sign(msgs[-1], sk)
+    finally:
+        eng.close()

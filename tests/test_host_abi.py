@@ -162,3 +162,20 @@ def test_ctypes_struct_layouts_match_the_headers(tmp_path):
         assert int(got[cname]) == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert int(got[cname + "." + f]) == getattr(py, f).offset, (cname, f)
+
+
+def test_tuning_file_round_trip(tmp_path):
+    """The autotuner's tab-separated tuning file (read by cuspx_create) keeps
+    one line per (GPU, set, op, bucket) and round-trips its mappings."""
+    from cuspx_gb300 import autotune
+    p = str(tmp_path / "t.tsv")
+    k1 = ("NVIDIA GB300", "sha256-128f-simple", "verify", 256)
+    k2 = ("NVIDIA GB300", "sha256-128f-simple", "sign", 1024)
+    autotune.save_entry(k1, 1.25, {"verify_item_max": 256, "verify_mode": 2}, p)
+    autotune.save_entry(k2, 20.5, {"leaf_block": 256}, p)
+    autotune.save_entry(k1, 1.0, {"verify_item_max": 0, "verify_mode": 2}, p)   # replaces
+    c = autotune.load_cache(p)
+    assert c == {k1: (1.0, {"verify_item_max": 0, "verify_mode": 2}), k2: (20.5, {"leaf_block": 256})}
+    lines = open(p).read().splitlines()
+    assert len(lines) == 2 and all(len(x.split("\t")) == 6 for x in lines)
+    assert [autotune.bucket(n) for n in (1, 2, 4, 5, 64, 65, 4096)] == [1, 4, 4, 16, 64, 256, 4096]

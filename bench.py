@@ -237,6 +237,10 @@ def main():
     # the ALU pipe alone (reported beside it)
     peak_ops, _ = c.int_peak(local, 8192, mix=1)
     peak_alu, _ = c.int_peak(local, 8192, mix=0)
+    # dependent SHA-256 compressions by warps per SM: the latency of one
+    # (1 warp) and how many warps the ALU pipe needs
+    cmp_curve = {w: {"cmp_per_s": r, "ns_per_cmp": ns}
+                 for w in (1, 4, 8, 16) for r, ns in [c.cmp_rate(w, local, 2048 if w <= 8 else 1024)]}
     # per-set launch mapping for this batch shape (autotuner, cached per GPU)
     from cuspx_gb300 import autotune
     tuned = {"sign": autotune.tune(eng, sid, c.OP_SIGN, count=BATCH, mlen=MLEN)[0],
@@ -337,6 +341,31 @@ def main():
         with open(tfile) as f:
             tj = json.load(f)
         traffic = tj.get("dram_bytes_per_launch_scaled_to_4096")
+
+    # ---- verify at 16384 items (4 copies of the batch): batch parallelism
+    # beside kernel quality -- the persistent kernel keeps ~4 warps per SM
+    # busy per 600 items, and the ALU pipe needs ~8 warps per SM
+    # (cuspx_cmp_rate) ----
+    verify16k = None
+    if rank == 0:
+        big = 4 * BATCH
+        vb4 = eng.batch(c.OP_VERIFY, sid, big, 4 * slab.nbytes, 1)
+        vb4.upload(big, pkb, 1, np.zeros(big, dtype=np.uint32), np.tile(slab, 4), 4 * slab.nbytes,
+                   np.arange(big, dtype=np.uint64) * MLEN, np.full(big, MLEN, dtype=np.uint64),
+                   np.tile(h_sigs[:BATCH * z["sig"]], 4))
+        t16 = []
+        for i in range(4):
+            flush.zero_()
+            torch.cuda.synchronize()
+            vb4.run(); vb4.sync()
+            if i:
+                t16.append(vb4.last_ms())
+        vv4 = np.zeros(big, dtype=np.int32)
+        vb4.download(None, None, vv4)
+        vb4.close()
+        v16 = big / (min(t16) / 1e3)
+        verify16k = {"value": v16, "unit": "verify/s", "items": big, "ms_per_batch": min(t16),
+                     "all_accept": bool((vv4 == 0).all()), "roofline_frac": int_frac(0, v16, peak_ops)}
 
     # ---- what the kernels execute, beside the model ----
     # The model counts the reference's structure at 1384 INT ops per
@@ -446,6 +475,8 @@ def main():
                        "mapping": tuned},
             "verify": {"value": verify_value, "unit": "verify/s", "ms_per_batch": verify_total / args.steps,
                        "roofline_frac": int_frac(0, verify_value, peak_ops)},
+            "verify_16384": verify16k,
+            "cmp_rate_by_warps_per_sm": cmp_curve,
             "step_roofline_frac": int_frac(value, 0, peak_ops),
             "compressions_per_s": value * (SIGN_CMP_128F + MSG_CMP_64B_SIGN),
             "executed": executed,

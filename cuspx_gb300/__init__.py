@@ -99,7 +99,7 @@ def lib():
     L.cuspx_int_peak.argtypes = [c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
     L.cuspx_int_peak_mix.argtypes = [c.c_int, c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_float)]
     L.cuspx_cmp_rate.argtypes = [c.c_int, c.c_int, c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double)]
-    L.cuspx_set_tuning_for.argtypes = [vp, c.c_int, c.c_int, sz, c.POINTER(Tuning)]
+    L.cuspx_set_tuning_for.argtypes = [vp, c.c_int, c.c_int, sz, sz, c.POINTER(Tuning)]
     L.cuspx_get_tuning_for.argtypes = [vp, c.c_int, c.c_int, sz, c.POINTER(Tuning)]
     L.cuspx_clear_tuning_for.argtypes = [vp, c.c_int, c.c_int]
     L.cuspx_load_tuning.argtypes = [vp, c.c_char_p]
@@ -209,13 +209,14 @@ class Engine:
         self._check(self.L.cuspx_get_tuning(self.h, sid, ctypes.byref(t)), "get_tuning")
         return t.as_dict()
 
-    def set_tuning_for(self, sid, op, max_count, **kw):
-        """Mapping of (set, op) for batches of at most max_count items (fields
-        not given keep the set's base mapping)."""
+    def set_tuning_for(self, sid, op, min_count, max_count, **kw):
+        """Mapping of (set, op) for batches of min_count..max_count items
+        (fields not given keep the set's base mapping)."""
         t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1)
         for k, v in kw.items():
             setattr(t, k, int(v))
-        self._check(self.L.cuspx_set_tuning_for(self.h, sid, op, max_count, ctypes.byref(t)), "set_tuning_for")
+        self._check(self.L.cuspx_set_tuning_for(self.h, sid, op, min_count, max_count, ctypes.byref(t)),
+                    "set_tuning_for")
 
     def get_tuning_for(self, sid, op, count):
         """The mapping a batch of `count` items of (set, op) runs with."""

@@ -17,10 +17,10 @@ best value kept, for two passes.  Every candidate is timed with CUDA events
 on the batch stream (min of `reps` runs after a warm-up).
 
 The result is installed in the library, not only in Python: the engine gets
-a per-size entry (cuspx_set_tuning_for) for batches of up to the bucket's
-size, and the result is appended to a tab-separated tuning file
-($CUSPX_TUNE_CACHE, default ~/.cache/cuspx/tune.tsv), one line per
-(GPU name, set, op, bucket).  cuspx_create reads that file, so every later
+a per-size entry (cuspx_set_tuning_for) for batches in the bucket's range
+(b/4 + 1 .. b items for the power of 4 b at or above the tuned count), and
+the result is written to a tab-separated tuning file ($CUSPX_TUNE_CACHE,
+default ~/.cache/cuspx/tune.tsv), one line per (GPU name, set, op, bucket).  cuspx_create reads that file, so every later
 context -- the api.h drop-ins, the one-shot calls and the serving loop
 included -- runs the tuned mappings without Python.
 """
@@ -53,24 +53,30 @@ def cache_path():
 
 
 def bucket(n):
-    """Batch-size bucket: the power of 4 at or above n."""
+    """Batch-size bucket: the power of 4 at or above n.  An entry tuned for
+    bucket b applies to batches of b/4 + 1 .. b items (1 item for b = 1)."""
     b = 1
     while b < n:
         b *= 4
     return b
 
 
+def bucket_range(b):
+    return (b // 4 + 1 if b > 1 else 1), b
+
+
 def load_cache(path=None):
-    """{(gpu, set, op, bucket): (ms, mapping)} from the tuning file."""
+    """{(gpu, set, op, bucket): (ms, mapping)} from the tuning file (one line
+    per entry: gpu, set, op, min_count, max_count = bucket, ms, knobs)."""
     out = {}
     try:
         with open(path or cache_path()) as f:
             for line in f:
                 col = line.rstrip("\n").split("\t")
-                if len(col) != 6:
+                if len(col) != 7:
                     continue
-                mapping = dict((k, int(v)) for k, v in (kv.split("=") for kv in col[5].split(",") if kv))
-                out[(col[0], col[1], col[2], int(col[3]))] = (float(col[4]), mapping)
+                mapping = dict((k, int(v)) for k, v in (kv.split("=") for kv in col[6].split(",") if kv))
+                out[(col[0], col[1], col[2], int(col[4]))] = (float(col[5]), mapping)
     except (OSError, ValueError):
         pass
     return out
@@ -86,8 +92,9 @@ def save_entry(key, ms, mapping, path=None):
         tmp = path + ".tmp"
         with open(tmp, "w") as f:
             for (gpu, sname, op, b), (m, mp) in sorted(cache.items()):
-                f.write("%s\t%s\t%s\t%d\t%.4f\t%s\n" % (gpu, sname, op, b, m,
-                                                        ",".join("%s=%d" % kv for kv in sorted(mp.items()))))
+                lo, hi = bucket_range(b)
+                f.write("%s\t%s\t%s\t%d\t%d\t%.4f\t%s\n" % (gpu, sname, op, lo, hi, m,
+                                                            ",".join("%s=%d" % kv for kv in sorted(mp.items()))))
         os.replace(tmp, path)
     except OSError:
         pass
@@ -117,7 +124,7 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2,
     if use_cache:
         hit = load_cache().get(key)
         if hit:
-            eng.set_tuning_for(sid, op, b, **hit[1])
+            eng.set_tuning_for(sid, op, *bucket_range(b), **hit[1])
             return hit[1], hit[0]
     z = set_sizes(sid)
     rng = np.random.default_rng(1234)
@@ -139,7 +146,7 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2,
     space = {k: [b if v is None else v for v in vals]
              for k, vals in (SIGN_SPACE if op == OP_SIGN else VERIFY_SPACE).items()}
     cur = {k: v for k, v in eng.get_tuning_for(sid, op, count).items() if k in space}
-    eng.set_tuning_for(sid, op, b, **cur)
+    eng.set_tuning_for(sid, op, *bucket_range(b), **cur)
     best_ms = _time(batch, reps)
     for _ in range(passes):
         improved = False
@@ -148,16 +155,16 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2,
                 if v == cur[knob]:
                     continue
                 trial = dict(cur, **{knob: v})
-                eng.set_tuning_for(sid, op, b, **trial)
+                eng.set_tuning_for(sid, op, *bucket_range(b), **trial)
                 ms = _time(batch, reps)
                 if verbose:
                     print("  %s=%s %.3f ms" % (knob, v, ms))
                 if ms < best_ms * 0.995:
                     best_ms, cur, improved = ms, trial, True
-            eng.set_tuning_for(sid, op, b, **cur)
+            eng.set_tuning_for(sid, op, *bucket_range(b), **cur)
         if not improved:
             break
-    eng.set_tuning_for(sid, op, b, **cur)
+    eng.set_tuning_for(sid, op, *bucket_range(b), **cur)
     batch.close()
     if op == OP_VERIFY:
         sb.close()

@@ -91,9 +91,9 @@ static const uint64_t kPairMsgBytes = 2048;
 
 struct OneshotJob;
 
-// a tuned mapping for batches of at most max_count items of one (set, op)
+// a tuned mapping for batches of min_count..max_count items of one (set, op)
 struct TuneEntry {
-    size_t max_count;
+    size_t min_count, max_count;
     Tuning t;
 };
 constexpr int kMaxTuneEntries = 16;
@@ -103,7 +103,7 @@ struct cuspx_ctx {
     std::mutex err_mu;   // err is written by any calling thread
     std::string err;
     Tuning tune[kNumSets];
-    // per-size entries (sorted by max_count) that take precedence over tune[]
+    // per-size entries (sorted by min_count) that take precedence over tune[]
     TuneEntry tune_for[kNumSets][3][kMaxTuneEntries];
     int ntune_for[kNumSets][3] = {};
     bool configured[2][3][2] = {};
@@ -218,14 +218,14 @@ static int cuda_fail(cuspx_ctx *ctx, cudaError_t e, const char *what) {
     } while (0)
 
 // The mapping a batch of `count` items of (set, op) runs with: the per-size
-// entry with the smallest max_count >= count (the largest entry for bigger
-// batches), else the set's base mapping.
+// entry whose range holds count, else the set's base mapping.
 static const Tuning &effective_tuning(const cuspx_ctx *ctx, int set, int op, size_t count) {
     const int ne = ctx->ntune_for[set][op];
-    if (ne == 0) return ctx->tune[set];
-    for (int i = 0; i < ne; i++)
-        if (count <= ctx->tune_for[set][op][i].max_count) return ctx->tune_for[set][op][i].t;
-    return ctx->tune_for[set][op][ne - 1].t;
+    for (int i = 0; i < ne; i++) {
+        const TuneEntry &e = ctx->tune_for[set][op][i];
+        if (count >= e.min_count && count <= e.max_count) return e.t;
+    }
+    return ctx->tune[set];
 }
 
 static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet);
@@ -400,22 +400,28 @@ int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *in) {
     return CUSPX_OK;
 }
 
-int cuspx_set_tuning_for(cuspx_ctx *ctx, int set, int op, size_t max_count, const cuspx_tuning *in) {
-    if (!ctx || !in || set < 0 || set >= kNumSets || op < 0 || op > 2 || max_count == 0) return CUSPX_EINVAL;
+int cuspx_set_tuning_for(cuspx_ctx *ctx, int set, int op, size_t min_count, size_t max_count,
+                         const cuspx_tuning *in) {
+    if (!ctx || !in || set < 0 || set >= kNumSets || op < 0 || op > 2 || min_count == 0 || max_count < min_count)
+        return CUSPX_EINVAL;
     std::lock_guard<std::mutex> lk(ctx->mu);
     Tuning t;
     if (int rc = merge_tuning(ctx, ctx->tune[set], in, t)) return rc;
     TuneEntry *e = ctx->tune_for[set][op];
     int &ne = ctx->ntune_for[set][op];
-    int i = 0;
-    while (i < ne && e[i].max_count < max_count) i++;
-    if (i < ne && e[i].max_count == max_count) {
-        e[i].t = t;
-        return CUSPX_OK;
+    for (int i = 0; i < ne; i++) {
+        if (e[i].min_count == min_count && e[i].max_count == max_count) {
+            e[i].t = t;   // the same range again: replace
+            return CUSPX_OK;
+        }
+        if (min_count <= e[i].max_count && e[i].min_count <= max_count)
+            return fail(ctx, CUSPX_EINVAL, "set_tuning_for: range overlaps an existing entry");
     }
     if (ne == kMaxTuneEntries) return fail(ctx, CUSPX_ENOMEM, "set_tuning_for: 16 entries per set and op");
+    int i = 0;
+    while (i < ne && e[i].min_count < min_count) i++;
     for (int j = ne; j > i; j--) e[j] = e[j - 1];
-    e[i] = TuneEntry{max_count, t};
+    e[i] = TuneEntry{min_count, max_count, t};
     ne++;
     return CUSPX_OK;
 }
@@ -475,7 +481,7 @@ int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *out) {
 
 // ---------------------------------------------------------------------------
 // tuning file (written by cuspx_gb300/autotune.py): one entry per line,
-//   <gpu name> TAB <set name> TAB <sign|verify|keygen> TAB <max_count> TAB <ms> TAB <knob>=<v>,<knob>=<v>...
+//   <gpu> TAB <set> TAB <sign|verify|keygen> TAB <min_count> TAB <max_count> TAB <ms> TAB <knob>=<v>,...
 // Lines of another GPU, unknown sets or knobs, and malformed lines are skipped.
 // ---------------------------------------------------------------------------
 static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
@@ -500,18 +506,18 @@ static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
             }
         }
         col.push_back(cur);
-        if (col.size() != 6 || col[0] != gpu) continue;
+        if (col.size() != 7 || col[0] != gpu) continue;
         const int set = set_by_name(col[1].c_str());
         const int op = col[2] == "sign" ? CUSPX_OP_SIGN : col[2] == "verify" ? CUSPX_OP_VERIFY
                                                         : col[2] == "keygen" ? CUSPX_OP_KEYGEN : -1;
-        const long long mc = atoll(col[3].c_str());
-        if (set < 0 || op < 0 || mc <= 0) continue;
+        const long long lo = atoll(col[3].c_str()), hi = atoll(col[4].c_str());
+        if (set < 0 || op < 0 || lo <= 0 || hi < lo) continue;
         cuspx_tuning t;
         t.leaf_block = t.fors_block = t.verify_block = t.tree_warps = t.chains_per_warp = t.verify_slots = 0;
         t.verify_mode = t.fors_lanes_log2 = t.tree_mode = t.chain_mode_max = t.verify_item_max = -1;
         bool ok = true;
         size_t at = 0;
-        const std::string &kv = col[5];
+        const std::string &kv = col[6];
         while (ok && at < kv.size()) {
             size_t end = kv.find(',', at);
             if (end == std::string::npos) end = kv.size();
@@ -537,7 +543,7 @@ static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
             else if (k == "verify_item_max") t.verify_item_max = v;
             else ok = false;
         }
-        if (ok && cuspx_set_tuning_for(ctx, set, op, (size_t)mc, &t) == CUSPX_OK) installed++;
+        if (ok && cuspx_set_tuning_for(ctx, set, op, (size_t)lo, (size_t)hi, &t) == CUSPX_OK) installed++;
     }
     fclose(f);
     return installed;

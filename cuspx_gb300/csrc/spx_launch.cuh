@@ -280,7 +280,8 @@ struct Family {
         if (tu.verify_item_max > 0 && A.count <= (uint32_t)tu.verify_item_max && P.hp <= 9) {
             // small batches: one item per block (its serial path sets the time)
             constexpr int LEN = 2 * N + 3, CW = (LEN + 31) / 32;
-            const size_t smem = (size_t)VerifyPolicy<HF>::slot_words(P.hp) * 4;
+            // one slot and the prefetched auth path of the next layer
+            const size_t smem = ((size_t)VerifyPolicy<HF>::slot_words(P.hp) + (size_t)P.hp * W) * 4;
             k_verify_item<HF><<<A.count, 32 * (CW + 1), smem, s>>>(P, A);
             CUSPX_MARK(pt, "k_verify_item", s);
             return;

@@ -1104,7 +1104,10 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
 // and sets its done bit; lane 0 of the last warp (the T warp) absorbs each
 // T block as soon as the chains it covers are done, then climbs the auth
 // path, and the T warp frames the next layer's stream.  One __syncthreads
-// per layer hands the root to the chain threads.  The chain threads never
+// per layer hands the root to the chain threads.  What a layer needs that
+// does not depend on the root of the layer below -- each chain's signature
+// value and step precompute, the auth path -- is fetched during the
+// previous layer, off the critical path.  The chain threads never
 // wait; the T lane's wait for done bits is bounded (kItemSpinLimit polls,
 // each after a short sleep): if it ever ran out the item's verdict is -3
 // and the layer loop ends at once.
@@ -1120,6 +1123,7 @@ __global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) 
     __shared__ int s_fail;
     uint32_t *S = smem;
     uint32_t *stream = S + PV::S_HDR;
+    uint32_t *pre_auth = smem + PV::slot_words(P.hp);   // next layer's auth path (h' x W words)
     const uint32_t tid = threadIdx.x, lane = tid & 31;
     const bool tw = (tid >> 5) == (uint32_t)CW;
     const uint32_t it = blockIdx.x;
@@ -1165,10 +1169,15 @@ __global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) 
             S[PV::S_MASK + 1] = PV::mask_init(1, LEN);
             S[PV::S_MASK + 2] = PV::mask_init(2, LEN);
         }
-        // the auth path of layer L
+        // the auth path of layer L, prefetched into pre_auth
         uint32_t *auth = stream + PV::kStreamWords;
-        const uint8_t *sl = sig + (uint64_t)L * (P.wots_bytes + P.hp * N);
-        for (int q = lane; q < P.hp * W; q += 32) auth[q] = reinterpret_cast<const uint32_t *>(sl + P.wots_bytes)[q];
+        for (int q = lane; q < P.hp * W; q += 32) auth[q] = pre_auth[q];
+    };
+    // T warp lanes: the auth path of layer L into pre_auth
+    auto fetch_auth = [&](int L, uint32_t from_lane) {
+        const uint8_t *sl = sig + (uint64_t)L * (P.wots_bytes + P.hp * N) + P.wots_bytes;
+        for (int q = (int)(lane - from_lane); q >= 0 && q < P.hp * W; q += 32 - from_lane)
+            pre_auth[q] = reinterpret_cast<const uint32_t *>(sl)[q];
     };
     // T lane: absorb the slot's stream block by block as its values arrive;
     // false if the wait ran out
@@ -1243,6 +1252,8 @@ __global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) 
             if (!run_t(root)) s_fail = 1;
 #pragma unroll
             for (int i = 0; i < W; i++) S[PV::S_ROOT + i] = root[i];
+        } else {
+            fetch_auth(0, 1);
         }
         __syncwarp();
         frame_layer(0);
@@ -1251,7 +1262,28 @@ __global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) 
 
     // ---- the d layers (wots_pk_from_sig + T_len + compute_root each) ----
     KeyRegs<N> key;
-    if (!tw && tid < LEN) key_from_work<HF>(key, pk, pk, *wk);
+    typename HF::FCtx fc;   // chain thread: the step precompute of its chain in the next layer
+    uint32_t nv[W];         // and that chain's signature value
+    // chain c of layer L: signature value and step precompute (neither
+    // depends on the root that sets the chain's length)
+    auto fetch_chain = [&](int L, int c) {
+        HF::load(nv, sig + (uint64_t)L * (P.wots_bytes + P.hp * N) + (uint64_t)c * N);
+        uint64_t tree_L;
+        uint32_t idx_L;
+        layer_index(P, tree, idx_leaf, L, tree_L, idx_L);
+        Adrs wa;
+        adrs_zero(wa);
+        adrs_layer(wa, L);
+        adrs_tree(wa, tree_L);
+        adrs_type(wa, ADDR_WOTS);
+        adrs_keypair(wa, idx_L);
+        adrs_chain(wa, c);
+        HF::f_prepare(fc, wa, key);
+    };
+    if (!tw && tid < LEN) {
+        key_from_work<HF>(key, pk, pk, *wk);
+        fetch_chain(0, (int)tid);
+    }
     for (int L = 0; L < P.d && !s_fail; L++) {
         if (!tw) {
             if (tid < LEN) {
@@ -1260,25 +1292,13 @@ __global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) 
 #pragma unroll
                 for (int i = 0; i < W; i++) root[i] = S[PV::S_ROOT + i];
                 const uint32_t ln = chain_len<HF>(P, root, c);
-                HF::load(v, sig + (uint64_t)L * (P.wots_bytes + P.hp * N) + (uint64_t)c * N);
-                if (ln < 15) {
-                    uint64_t tree_L;
-                    uint32_t idx_L;
-                    layer_index(P, tree, idx_leaf, L, tree_L, idx_L);
-                    Adrs wa;
-                    adrs_zero(wa);
-                    adrs_layer(wa, L);
-                    adrs_tree(wa, tree_L);
-                    adrs_type(wa, ADDR_WOTS);
-                    adrs_keypair(wa, idx_L);
-                    adrs_chain(wa, c);
-                    typename HF::FCtx fc;
-                    HF::f_prepare(fc, wa, key);
-                    for (uint32_t s = ln; s < 15; s++) HF::f_step(v, v, fc, s, key);
-                }
+#pragma unroll
+                for (int i = 0; i < W; i++) v[i] = nv[i];
+                for (uint32_t s = ln; s < 15; s++) HF::f_step(v, v, fc, s, key);
                 PV::write_value(stream, c, v);
                 __threadfence_block();   // the value before its done bit
                 PV::mark_done(S, c);
+                if (L + 1 < P.d) fetch_chain(L + 1, c);
             }
         } else {
             if (lane == 0) {
@@ -1298,6 +1318,8 @@ __global__ void __launch_bounds__(128) k_verify_item(SetParams P, VerifyArgs A) 
 #pragma unroll
                     for (int i = 0; i < W; i++) S[PV::S_ROOT + i] = v[i];
                 }
+            } else if (L + 1 < P.d) {
+                fetch_auth(L + 1, 1);   // while lane 0 absorbs T and climbs
             }
             __syncwarp();
             if (L + 1 < P.d && !s_fail) frame_layer(L + 1);

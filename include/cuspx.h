@@ -86,21 +86,22 @@ typedef struct {
 int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
 int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
 /* Mappings by batch size (what the autotuner installs): the mapping of
- * `set` for `op` batches of at most max_count items, built from the set's
- * current base mapping with t's fields applied (cuspx_set_tuning's rules).
- * A batch of `count` items runs with the entry of smallest max_count >=
- * count (the largest entry for bigger batches), or with the base mapping
- * when (set, op) has no entry.  Entries take precedence over the base;
- * at most 16 per (set, op).  Change mappings while no batch of the set is
- * being launched. */
-int cuspx_set_tuning_for(cuspx_ctx *ctx, int set, int op, size_t max_count, const cuspx_tuning *t);
+ * `set` for `op` batches of min_count..max_count items (inclusive), built
+ * from the set's current base mapping with t's fields applied
+ * (cuspx_set_tuning's rules).  A batch runs with the entry whose range holds
+ * its item count, or with the base mapping if none does.  Ranges of one
+ * (set, op) may not overlap (the same range again replaces its entry); at
+ * most 16 per (set, op).  Change mappings while no batch of the set is being
+ * launched. */
+int cuspx_set_tuning_for(cuspx_ctx *ctx, int set, int op, size_t min_count, size_t max_count,
+                         const cuspx_tuning *t);
 /* the mapping a batch of `count` items of (set, op) runs with */
 int cuspx_get_tuning_for(cuspx_ctx *ctx, int set, int op, size_t count, cuspx_tuning *t);
 /* drop the entries of (set, op), or of every op when op < 0 */
 int cuspx_clear_tuning_for(cuspx_ctx *ctx, int set, int op);
 /* Install the entries of a tuning file written by the autotuner
  * (cuspx_gb300/autotune.py): one tab-separated line per entry,
- *   <gpu name> <set name> <sign|verify|keygen> <max_count> <ms> <knob>=<v>,...
+ *   <gpu name> <set name> <sign|verify|keygen> <min_count> <max_count> <ms> <knob>=<v>,...
  * Lines of other GPUs are skipped.  cuspx_create reads $CUSPX_TUNE_CACHE
  * (default $HOME/.cache/cuspx/tune.tsv) when it exists, so the api.h
  * drop-ins, the one-shot calls and serving all run the tuned mappings.

@@ -55,8 +55,10 @@ def test_tune_is_installed_in_the_library_and_round_trips(tmp_path, monkeypatch)
     try:
         got = eng2.get_tuning_for(sid, c.OP_VERIFY, n)
         assert {k: got[k] for k in mapping} == mapping
-        # sizes above the largest entry take it too; other ops and sets keep their base
-        assert {k: eng2.get_tuning_for(sid, c.OP_VERIFY, 5000)[k] for k in mapping} == mapping
+        # sizes outside the entry's bucket (65..256 items) and other ops keep the base mapping
+        assert eng2.get_tuning_for(sid, c.OP_VERIFY, 64) == eng2.get_tuning(sid)
+        assert eng2.get_tuning_for(sid, c.OP_VERIFY, 257) == eng2.get_tuning(sid)
+        assert {k: eng2.get_tuning_for(sid, c.OP_VERIFY, 65)[k] for k in mapping} == mapping
         assert eng2.get_tuning_for(sid, c.OP_SIGN, n) == eng2.get_tuning(sid)
         eng2.clear_tuning_for(sid)
         assert eng2.get_tuning_for(sid, c.OP_VERIFY, n) == eng2.get_tuning(sid)
@@ -65,18 +67,21 @@ def test_tune_is_installed_in_the_library_and_round_trips(tmp_path, monkeypatch)
         eng2.close()
 
 
-def test_per_size_entries_pick_the_smallest_cover(monkeypatch, tmp_path):
+def test_per_size_entries_cover_their_ranges(monkeypatch, tmp_path):
     import cuspx_gb300 as c
     monkeypatch.setenv("CUSPX_TUNE_CACHE", str(tmp_path / "none.tsv"))
     eng = c.Engine(0)
     try:
         sid = c.set_id("shake256-128f-simple")
-        eng.set_tuning_for(sid, c.OP_SIGN, 64, leaf_block=64)
-        eng.set_tuning_for(sid, c.OP_SIGN, 1024, leaf_block=256)
+        base = eng.get_tuning(sid)["leaf_block"]
+        eng.set_tuning_for(sid, c.OP_SIGN, 1, 64, leaf_block=64)
+        eng.set_tuning_for(sid, c.OP_SIGN, 65, 1024, leaf_block=256)
         assert eng.get_tuning_for(sid, c.OP_SIGN, 1)["leaf_block"] == 64
         assert eng.get_tuning_for(sid, c.OP_SIGN, 64)["leaf_block"] == 64
         assert eng.get_tuning_for(sid, c.OP_SIGN, 65)["leaf_block"] == 256
-        assert eng.get_tuning_for(sid, c.OP_SIGN, 99999)["leaf_block"] == 256
+        assert eng.get_tuning_for(sid, c.OP_SIGN, 99999)["leaf_block"] == base
+        with pytest.raises(c.CuspxError):   # overlaps 65..1024
+            eng.set_tuning_for(sid, c.OP_SIGN, 1000, 2000, leaf_block=128)
         # every entry gives the oracle's bytes
         import spx_oracle
         o = spx_oracle.Oracle("shake256-128f-simple")

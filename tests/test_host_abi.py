@@ -177,5 +177,8 @@ def test_tuning_file_round_trip(tmp_path):
     c = autotune.load_cache(p)
     assert c == {k1: (1.0, {"verify_item_max": 0, "verify_mode": 2}), k2: (20.5, {"leaf_block": 256})}
     lines = open(p).read().splitlines()
-    assert len(lines) == 2 and all(len(x.split("\t")) == 6 for x in lines)
+    assert len(lines) == 2 and all(len(x.split("\t")) == 7 for x in lines)
+    # each line carries its bucket's item range: 1024 -> 257..1024, 256 -> 65..256
+    assert sorted(tuple(x.split("\t")[3:5]) for x in lines) == [("257", "1024"), ("65", "256")]
     assert [autotune.bucket(n) for n in (1, 2, 4, 5, 64, 65, 4096)] == [1, 4, 4, 16, 64, 256, 4096]
+    assert [autotune.bucket_range(b) for b in (1, 4, 64)] == [(1, 1), (2, 4), (17, 64)]

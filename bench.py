@@ -621,11 +621,13 @@ def served_runs(c, eng, peak_ops, peak_alu, seconds=2.0):
     out["served_128f"] = pts
     names = ["sha256-128f-simple", "sha256-192f-simple", "shake256-256f-simple"]
     sids = [c.set_id(n) for n in names]
-    # admission budget: device bytes of pending plus in-flight requests; at
-    # ~15 GB/s of admitted bytes when saturated, 2 GiB bounds the queue ahead
-    # of a request to ~0.15 s of work
-    budget = 2 << 30
-    srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000, mem_budget=budget)
+    # admission: device bytes of pending plus in-flight requests within 2 GiB,
+    # and at most 50 ms of estimated GPU work queued or in flight (requests
+    # beyond either are refused at submission); a launch carries at most
+    # 20 ms of work, so a batch of SHAKE-256-256f signs stays short
+    budget, queue_ms, launch_ms = 2 << 30, 50.0, 20.0
+    srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000, mem_budget=budget, max_queue_ms=queue_ms,
+                   max_launch_ms=launch_ms)
     per = 1024 // len(sids) + 1
     stream_keys = {}
     for s2 in sids:
@@ -656,7 +658,7 @@ def served_runs(c, eng, peak_ops, peak_alu, seconds=2.0):
                     "oracle_sample": {"signatures": len(r["samples"]), "identical": sample_ok}})
     srv.close()
     out["served_stream"] = {"sets": names, "keys": per * len(sids), "lengths": "log-uniform 16 B..1 MiB",
-                            "mem_budget_bytes": budget,
+                            "mem_budget_bytes": budget, "max_queue_ms": queue_ms, "max_launch_ms": launch_ms,
                             "oracle_sample": "1 in 64 timed signs kept (up to 12 per point), byte-compared "
                                              "with the CPU oracle",
                             "points": pts}

@@ -41,7 +41,8 @@ class Tuning(ctypes.Structure):
     """cuspx_tuning: the launch mapping of one parameter set."""
     _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
                                             "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode",
-                                            "chain_mode_max", "verify_slots", "verify_item_max")]
+                                            "chain_mode_max", "verify_slots", "verify_item_max",
+                                            "verify_claim_min")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -199,7 +200,7 @@ class Engine:
 
     def set_tuning(self, sid, **kw):
         """Change fields of a set's launch mapping (others keep their value)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1, 0)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")
@@ -212,7 +213,7 @@ class Engine:
     def set_tuning_for(self, sid, op, min_count, max_count, **kw):
         """Mapping of (set, op) for batches of min_count..max_count items
         (fields not given keep the set's base mapping)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1, 0)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning_for(self.h, sid, op, min_count, max_count, ctypes.byref(t)),
@@ -411,7 +412,9 @@ E_BUSY, E_TIMEDOUT, E_NOMEM = -4, -5, -3
 
 class ServeConfig(ctypes.Structure):
     _fields_ = [("mem_budget", ctypes.c_size_t), ("max_batch", ctypes.c_int), ("max_inflight", ctypes.c_int),
-                ("window_us", ctypes.c_int), ("max_keys", ctypes.c_int), ("max_queue", ctypes.c_size_t)]
+                ("window_us", ctypes.c_int), ("max_keys", ctypes.c_int), ("max_queue", ctypes.c_size_t),
+                ("max_queue_ms", ctypes.c_double), ("max_launch_ms", ctypes.c_double),
+                ("gpu_ops_per_s", ctypes.c_double)]
 
 
 class ServeCounters(ctypes.Structure):
@@ -498,10 +501,12 @@ def _bind_serve(L):
 class Server:
     """A serving loop on one engine context (cuspx_serve_*)."""
 
-    def __init__(self, eng, mem_budget=0, max_batch=0, max_inflight=0, window_us=0, max_keys=0, max_queue=0):
+    def __init__(self, eng, mem_budget=0, max_batch=0, max_inflight=0, window_us=0, max_keys=0, max_queue=0,
+                 max_queue_ms=0.0, max_launch_ms=0.0, gpu_ops_per_s=0.0):
         self.eng = eng
         self.L = _bind_serve(eng.L)
-        cfg = ServeConfig(mem_budget, max_batch, max_inflight, window_us, max_keys, max_queue)
+        cfg = ServeConfig(mem_budget, max_batch, max_inflight, window_us, max_keys, max_queue, max_queue_ms,
+                          max_launch_ms, gpu_ops_per_s)
         h = ctypes.c_void_p()
         eng._check(self.L.cuspx_serve_create(eng.h, ctypes.byref(cfg), ctypes.byref(h)), "serve_create")
         self.h = h

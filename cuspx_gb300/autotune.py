@@ -20,7 +20,8 @@ The result is installed in the library, not only in Python: the engine gets
 a per-size entry (cuspx_set_tuning_for) for batches in the bucket's range
 (b/4 + 1 .. b items for the power of 4 b at or above the tuned count), and
 the result is written to a tab-separated tuning file ($CUSPX_TUNE_CACHE,
-default ~/.cache/cuspx/tune.tsv), one line per (GPU name, set, op, bucket).  cuspx_create reads that file, so every later
+default ~/.cache/cuspx/tune.tsv), one line per (GPU name, set, op, bucket).
+cuspx_create reads that file, so every later
 context -- the api.h drop-ins, the one-shot calls and the serving loop
 included -- runs the tuned mappings without Python.
 """

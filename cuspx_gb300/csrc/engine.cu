@@ -385,6 +385,10 @@ static int merge_tuning(cuspx_ctx *ctx, const Tuning &base, const cuspx_tuning *
         t.verify_slots = in->verify_slots;
     }
     if (in->verify_item_max >= 0) t.verify_item_max = in->verify_item_max;
+    if (in->verify_claim_min > 0) {
+        if (in->verify_claim_min > 32) return fail(ctx, CUSPX_EINVAL, "verify_claim_min must be in 1..32");
+        t.verify_claim_min = in->verify_claim_min;
+    }
     out = t;
     return CUSPX_OK;
 }
@@ -446,6 +450,7 @@ static void to_abi(const Tuning &t, cuspx_tuning *out) {
     out->chain_mode_max = t.chain_mode_max;
     out->verify_slots = t.verify_slots;
     out->verify_item_max = t.verify_item_max;
+    out->verify_claim_min = t.verify_claim_min;
 }
 
 int cuspx_get_tuning_for(cuspx_ctx *ctx, int set, int op, size_t count, cuspx_tuning *out) {
@@ -515,6 +520,7 @@ static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
         cuspx_tuning t;
         t.leaf_block = t.fors_block = t.verify_block = t.tree_warps = t.chains_per_warp = t.verify_slots = 0;
         t.verify_mode = t.fors_lanes_log2 = t.tree_mode = t.chain_mode_max = t.verify_item_max = -1;
+        t.verify_claim_min = 0;
         bool ok = true;
         size_t at = 0;
         const std::string &kv = col[6];
@@ -541,6 +547,7 @@ static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
             else if (k == "chain_mode_max") t.chain_mode_max = v;
             else if (k == "verify_slots") t.verify_slots = v;
             else if (k == "verify_item_max") t.verify_item_max = v;
+            else if (k == "verify_claim_min") t.verify_claim_min = v;
             else ok = false;
         }
         if (ok && cuspx_set_tuning_for(ctx, set, op, (size_t)lo, (size_t)hi, &t) == CUSPX_OK) installed++;

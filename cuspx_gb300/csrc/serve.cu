@@ -58,6 +58,7 @@ struct Req {
     bool waiting = false;   // a thread is in cuspx_serve_wait on this request
     unsigned flags = 0;
     size_t admit_bytes = 0; // device bytes counted against the budget at submit
+    double work_ops = 0;    // estimated integer ops of its hashing
     Clock::time_point t0, t1;
 };
 
@@ -70,6 +71,7 @@ struct KeyTable {
 struct Slot {
     cuspx_batch *b = nullptr;
     size_t cap = 0, msg_cap = 0;
+    double work = 0;   // estimated ops of the launch in flight
     uint8_t *h_msg = nullptr;
     uint64_t *h_off = nullptr, *h_len = nullptr, *h_siglen = nullptr;
     uint32_t *h_kidx = nullptr;
@@ -121,8 +123,32 @@ struct Group {
     std::deque<Req *> pending;
     std::vector<Slot *> slots;
     size_t per_item = 0;
+    double item_ops = 0;   // estimated integer ops of one request, message hashing excluded
     SetParams P{};
 };
+
+// Expected hash units of one operation of a set, message hashing excluded,
+// counted the way the reference runs it (crypto_sign_signature,
+// crypto_sign_verify): the model the benchmark's roofline fractions use.
+// The WOTS+ digit sum is its expectation over random messages: 7.5 per
+// message digit, about 7.5 for the two low checksum digits and 15n / 256
+// for the top one.
+void op_units(const SetDesc &sd, double &sign, double &verify, double &ops_per_unit) {
+    const int n = sd.n, hp = sd.h / sd.d, a = sd.a, k = sd.k, d = sd.d, ln = 2 * n + 3;
+    const bool shake = sd.hash == 1, robust = sd.robust != 0;
+    auto th = [&](int m) -> double {
+        if (shake) return (n + 32 + m * n) / 136 + 1 + (robust ? (m * n + 135) / 136 : 0);
+        return (22 + m * n + 9 + 63) / 64 + (robust ? ((m * n + 31) / 32) * ((n + 26 + 9 + 63) / 64) : 0);
+    };
+    const double F = th(1), H = th(2), prf = 1, seed = shake ? 0 : 1;
+    const double leaf = ln * (prf + 15 * F) + th(ln);
+    const double xmss = (double)(1 << hp) * leaf + ((1 << hp) - 1) * H;
+    const double e = 2 * n * 7.5 + 7.5 + 7.5 + 15.0 * n / 256.0;
+    sign = seed + k * (prf + (double)(1 << a) * (prf + F) + ((1 << a) - 1) * H) + th(k) + d * xmss +
+           d * (ln * prf + e * F);
+    verify = seed + k * (F + a * H) + th(k) + d * (th(ln) + hp * H) + d * (ln * 15 - e) * F;
+    ops_per_unit = shake ? 4560.0 : 1384.0;
+}
 
 // Latency histogram: bin i holds [2^(i/64), 2^((i+1)/64)) microseconds
 // (1.1% wide), from 1 us to 2^31 us; a percentile is read as the
@@ -183,6 +209,7 @@ struct cuspx_server {
     std::unordered_map<uint64_t, Req *> live;
     uint64_t next_ticket = 1;
     size_t pending_total = 0, pending_bytes = 0, bytes_inflight = 0, bytes_peak = 0;
+    double work_queued = 0;   // estimated ops of the requests pending or in flight
     uint64_t submitted = 0, completed = 0, refused = 0, failed = 0, launches = 0, batched = 0;
     uint64_t sign_done = 0, verify_done = 0, wrong = 0;
     double launch_ms_sum = 0, launch_ms_max = 0;
@@ -342,6 +369,9 @@ static void finish_slot(cuspx_server *s, Group &g, Slot *sl, bool ok) {
     sl->reqs.clear();
     if (sl->stream >= 0) s->stream_load[g.cls][sl->stream]--;
     sl->stream = -1;
+    s->work_queued -= sl->work;
+    if (s->work_queued < 0) s->work_queued = 0;
+    sl->work = 0;
     s->bytes_inflight -= sl->bytes;
     sl->bytes = 0;
     sl->busy = false;
@@ -404,13 +434,17 @@ static void scheduler(cuspx_server *s, int lc) {
                 // (their device bytes were admitted against the budget when
                 // they were submitted, so pending + in-flight stays within it)
                 size_t n = 0, bytes = 0, mbytes = 0;
+                double work = 0;
                 const size_t mcap = class_msg_bytes(s, g);
+                const double wcap = s->cfg.max_launch_ms > 0 ? s->cfg.max_launch_ms * 1e-3 * s->cfg.gpu_ops_per_s : 0;
                 for (Req *r : g.pending) {
                     if (n == items) break;
                     const size_t m16 = (r->mlen + 15) & ~(size_t)15;
                     if (mbytes + m16 > mcap) break;
+                    if (wcap > 0 && n > 0 && work + r->work_ops > wcap) break;
                     mbytes += m16;
                     bytes += r->admit_bytes;
+                    work += r->work_ops;
                     n++;
                 }
                 if (n == 0) break;
@@ -422,6 +456,7 @@ static void scheduler(cuspx_server *s, int lc) {
                 s->pending_bytes -= bytes;
                 free_sl->busy = true;
                 free_sl->bytes = bytes;
+                free_sl->work = work;
                 {
                     // the class's least loaded stream
                     std::vector<int> &load = s->stream_load[g.cls];
@@ -462,6 +497,14 @@ int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_serv
     if (s->cfg.max_keys <= 0) s->cfg.max_keys = 4096;
     if (!s->cfg.max_queue) s->cfg.max_queue = 1u << 20;
     cudaGetDevice(&s->device);
+    if (s->cfg.gpu_ops_per_s <= 0 && (s->cfg.max_queue_ms > 0 || s->cfg.max_launch_ms > 0)) {
+        // 60% of the SHA-256-round peak: about what the served three-set
+        // stream reaches at saturation
+        double peak = 0;
+        float ms = 0;
+        if (cuspx_int_peak_mix(s->device, 1024, 1, &peak, &ms) != CUSPX_OK || peak <= 0) peak = 2e13;
+        s->cfg.gpu_ops_per_s = 0.6 * peak;
+    }
     s->keys.resize(kNumSets);
     s->groups.resize(2 * kNumSets * kClasses);
     for (int op = 1; op <= 2; op++)
@@ -473,6 +516,9 @@ int cuspx_serve_create(cuspx_ctx *ctx, const cuspx_serve_config *cfg, cuspx_serv
                 g.cls = lc;
                 g.P = make_params(kSets[set]);
                 g.per_item = item_bytes(op, g.P);
+                double su, vu, opu;
+                op_units(kSets[set], su, vu, opu);
+                g.item_ops = (op == CUSPX_OP_SIGN ? su : vu) * opu;
             }
     // short-message launches run ahead of middle ones, those ahead of long
     // ones on the GPU (lo is the least urgent priority, hi the most)
@@ -620,6 +666,11 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     const KeyTable &kt = s->keys[set];
     Group &g = s->group(op, set, class_of(mlen));
     r->admit_bytes = g.per_item + ((mlen + 15) & ~(size_t)15);
+    {
+        double su, vu, opu;
+        op_units(kSets[set], su, vu, opu);
+        r->work_ops = g.item_ops + msg_units(op, kSets[set], g.P, mlen) * opu;
+    }
     int rc = CUSPX_OK;
     if (s->stop) rc = CUSPX_EBUSY;
     else if (key_id >= kt.n || (op == CUSPX_OP_SIGN && !kt.has_sk[key_id])) rc = CUSPX_EINVAL;
@@ -629,6 +680,12 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     // admission by device-memory budget: the bytes of everything pending or
     // in flight, this request included
     else if (s->pending_bytes + s->bytes_inflight + r->admit_bytes > s->cfg.mem_budget) rc = CUSPX_EBUSY;
+    // admission by queued work: what is pending or in flight, in ms of the
+    // device's capacity (a request is admitted into an empty queue whatever
+    // its size)
+    else if (s->cfg.max_queue_ms > 0 && s->work_queued > 0 &&
+             (s->work_queued + r->work_ops) / s->cfg.gpu_ops_per_s * 1e3 > s->cfg.max_queue_ms)
+        rc = CUSPX_EBUSY;
     if (rc != CUSPX_OK) {
         s->refused++;
         lk.unlock();
@@ -641,6 +698,7 @@ static int submit(cuspx_server *s, int op, int set, uint32_t key_id, const uint8
     g.pending.push_back(r);
     s->pending_total++;
     s->pending_bytes += r->admit_bytes;
+    s->work_queued += r->work_ops;
     s->submitted++;
     if (ticket) *ticket = r->ticket;
     const bool kick = g.pending.size() == 1 || g.pending.size() >= class_items(s, g);

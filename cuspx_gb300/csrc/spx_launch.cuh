@@ -27,6 +27,7 @@ struct Tuning {
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
     int verify_slots = 4;    // most items per warp in the persistent verify kernel
     int verify_item_max = 0; // batches of at most this many items verify one item per block
+    int verify_claim_min = 1;// persistent verify: free lanes before chains are handed out
 };
 
 struct KeygenArgs {
@@ -182,7 +183,8 @@ struct Family {
             const uint64_t want = ceil_div(A.count, (uint64_t)G * wpb);
             const uint64_t cap = (uint64_t)occ * (sms > 0 ? sms : 1);
             cudaMemsetAsync(A.ctr, 0, sizeof(uint32_t), s);
-            k_verify_hyper<HF><<<(unsigned)(want < cap ? want : cap), 32 * wpb, smem, s>>>(P, A, A.ctr, G);
+            const int claim_min = tu.verify_claim_min < 1 ? 1 : (tu.verify_claim_min > 32 ? 32 : tu.verify_claim_min);
+            k_verify_hyper<HF><<<(unsigned)(want < cap ? want : cap), 32 * wpb, smem, s>>>(P, A, A.ctr, G, claim_min);
             CUSPX_MARK(pt, "k_verify_hyper", s);
         }
     }

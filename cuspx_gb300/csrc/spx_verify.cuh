@@ -798,7 +798,8 @@ using VerifyPolicy = typename std::conditional<
     typename std::conditional<HF::kRobust, VerifySha2Robust<HF>, VerifySha2<HF>>::type>::type;
 
 template <class HF>
-__global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A, uint32_t *ctr, int G) {
+__global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A, uint32_t *ctr, int G,
+                                                      int claim_min) {
     using PV = VerifyPolicy<HF>;
     constexpr int W = PV::W, N = PV::N, LEN = PV::LEN;
     extern __shared__ uint32_t smem[];
@@ -826,6 +827,10 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
     // out, so the claim loop reads nothing for the others (SHA-256-128f at
     // 4096 items -2.3%, robust SHAKE-256f -8%)
     uint32_t open = 0;
+    // warp-uniform: slots whose T stream has no lane yet (the critical path:
+    // always claimed at once); chains are handed out only once at least
+    // claim_min lanes are free, so the claim pass runs less often
+    uint32_t tpend = 0;
 
     while (true) {
         // ---- slot upkeep: refill empty slots, set up layers (warp-uniform) ----
@@ -875,6 +880,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                     S[PV::S_STATE] = PV::ACTIVE;
                 }
                 open |= 1u << g;
+                tpend |= 1u << g;
                 __syncwarp();
             }
             if (S[PV::S_STATE] == PV::ADVANCE) {
@@ -925,6 +931,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                     S[PV::S_STATE] = PV::ACTIVE;
                 }
                 open |= 1u << g;
+                tpend |= 1u << g;
                 __syncwarp();
             }
         }
@@ -933,7 +940,8 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         // ---- task claims (warp-uniform; slot order is priority order, and
         // within a slot the T stream -- the critical path -- comes first) ----
         uint32_t need = __ballot_sync(0xffffffffu, kind == PV::K_NONE);
-        for (uint32_t om = open; om && need; om &= om - 1) {
+        const bool chain_claims = __popc(need) >= claim_min;
+        for (uint32_t om = open & (chain_claims ? ~0u : tpend); om && need; om &= om - 1) {
             const int g = __ffs(om) - 1;
             uint32_t *S = slots + g * SW;
             if (S[PV::S_STATE] != PV::ACTIVE) {
@@ -952,11 +960,12 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
                 }
                 __syncwarp();
                 if (lane == 0) S[PV::S_TCLAIM] = 1;
+                tpend &= ~(1u << g);
                 __syncwarp();
                 need &= ~(1u << leader);
             }
             const uint8_t *lens = reinterpret_cast<const uint8_t *>(S + PV::S_LENS);
-            while (need) {
+            while (need && chain_claims) {
                 const int next = (int)S[PV::S_NEXT];
                 if (next >= LEN) break;
                 const int rank = __popc(need & lt_mask);
@@ -985,7 +994,7 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
             // lanes still free: every chain of the slot is handed out; with
             // the T stream taken too there is nothing more until the slot's
             // next layer (set again by the upkeep)
-            if (need && S[PV::S_TCLAIM] != 0) open &= ~(1u << g);
+            if (chain_claims && need && S[PV::S_TCLAIM] != 0) open &= ~(1u << g);
         }
         if (!__any_sync(0xffffffffu, kind != PV::K_NONE)) break;
 

@@ -80,6 +80,9 @@ typedef struct {
     int verify_item_max;  /* verify batches of at most this many items (any verify_mode) with one
                              thread block per item: a thread per WOTS+ chain and a T lane that
                              streams T_len behind the chains (0: never) */
+    int verify_claim_min; /* verify_mode 2: WOTS+ chains are handed out to free lanes once at
+                             least this many lanes of a warp are free (1..32; T streams always
+                             at once) */
 } cuspx_tuning;
 /* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2,
  * tree_mode, chain_mode_max and verify_item_max, which keep it when < 0 */

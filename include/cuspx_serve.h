@@ -52,6 +52,19 @@ typedef struct {
     int window_us;       /* batching window (0: 500 us) */
     int max_keys;        /* resident keys per set (0: 4096) */
     size_t max_queue;    /* pending requests before submit refuses (0: 1<<20) */
+    /* Work-based limits (0: off).  A request's GPU work is estimated from its
+     * parameter set's hash units (the reference's sign / verify structure)
+     * and its message length, in milliseconds of the device's hashing
+     * capacity (gpu_ops_per_s).  max_queue_ms refuses a submission with
+     * CUSPX_EBUSY when the work pending or in flight would exceed it, which
+     * bounds the queueing delay at overload; max_launch_ms caps the work of
+     * one launch (at least one request), so a batch of heavy requests
+     * (SHAKE-256-256f signs: ~0.1 ms of the whole GPU each) does not keep
+     * its group's next requests waiting for long. */
+    double max_queue_ms;
+    double max_launch_ms;
+    double gpu_ops_per_s;   /* integer ops per second the estimates assume (0: 60% of the
+                               measured SHA-256-round peak, cuspx_int_peak_mix) */
 } cuspx_serve_config;
 
 typedef struct {

@@ -160,8 +160,10 @@ def test_verify_mappings_agree(engine, setname):
                   {"verify_mode": 0, "chains_per_warp": 1024}, {"verify_mode": 1},
                   {"verify_mode": 2, "verify_slots": 1, "verify_block": 32},
                   {"verify_mode": 2, "verify_slots": 3, "verify_block": 64},
-                  {"verify_mode": 2, "verify_slots": 8, "verify_block": 128}):
-            engine.set_tuning(sid, verify_item_max=0, **m)
+                  {"verify_mode": 2, "verify_slots": 8, "verify_block": 128},
+                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 64, "verify_claim_min": 6},
+                  {"verify_mode": 2, "verify_slots": 2, "verify_block": 32, "verify_claim_min": 32}):
+            engine.set_tuning(sid, verify_item_max=0, verify_claim_min=1, **m)
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
             assert list(got) == want, m
         # one item per block (the small-batch kernel)
@@ -172,6 +174,8 @@ def test_verify_mappings_agree(engine, setname):
         # same batch one item per block (several blocks share each SM)
         rep = 1300
         for m in ({"verify_mode": 2, "verify_slots": 8, "verify_block": 64, "verify_item_max": 0},
+                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 64, "verify_item_max": 0,
+                   "verify_claim_min": 8},
                   {"verify_item_max": 2000}):
             engine.set_tuning(sid, **m)
             got = engine.verify_batch(sid, [pks[kidx[i % 12]] for i in range(rep)],

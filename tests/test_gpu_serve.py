@@ -314,3 +314,47 @@ def test_loadgen_sample_matches_oracle(engine):
             assert sig == oracles[sid].sign(msg, keys[sid][1][kid]), (sid, len(msg))
     finally:
         srv.close()
+
+
+def test_work_based_admission_and_launch_cap(engine):
+    """With max_queue_ms the server refuses a submission once the estimated
+    GPU work pending or in flight exceeds that many ms of the stated capacity
+    (here 1e13 integer ops/s: one SHAKE-256-256f sign is ~1.6e9 ops, 0.16 ms);
+    with max_launch_ms a launch carries at most that much work.  Every
+    admitted request completes with the right bytes."""
+    import cuspx_gb300 as c
+    import spx_oracle
+    name = "shake256-256f-simple"
+    sid = c.set_id(name)
+    keys = _setup(engine, [name], 1, seed=61)
+    pks, sks, z = keys[sid]
+    srv = c.Server(engine, max_batch=256, max_inflight=1, window_us=100_000, max_queue_ms=1.0,
+                   max_launch_ms=0.35, gpu_ops_per_s=1e13)
+    try:
+        for op in (c.OP_SIGN, c.OP_VERIFY):
+            srv.prepare(op, sid)
+        kid = srv.add_keys(sid, sks)[0]
+        ts, refused = [], 0
+        for i in range(40):
+            try:
+                ts.append((i, srv.submit(c.OP_SIGN, sid, kid, b"w%d" % i)))
+            except c.CuspxError as e:
+                assert e.code == c.E_BUSY
+                refused += 1
+        # ~1 ms / 0.16 ms per sign: about six admitted while the first ones run
+        assert 3 <= len(ts) <= 16 and refused >= 24, (len(ts), refused)
+        sigs = {}
+        for i, t in ts:
+            sig, st, _ = srv.wait(t, 120_000_000, z["sig"])
+            assert st == 0
+            sigs[i] = sig
+        s = srv.stats()
+        # 0.35 ms per launch: at most two of these signs in one launch
+        assert s["launches"] >= (len(ts) + 1) // 2, s
+        i0 = ts[0][0]
+        assert sigs[i0] == spx_oracle.Oracle(name).sign(b"w%d" % i0, sks[0])
+        # drained: admitted again
+        t = srv.submit(c.OP_SIGN, sid, kid, b"again")
+        assert srv.wait(t, 120_000_000, z["sig"])[1] == 0
+    finally:
+        srv.close()

@@ -163,7 +163,7 @@ def test_verify_mappings_agree(engine, setname):
                   {"verify_mode": 2, "verify_slots": 8, "verify_block": 128},
                   {"verify_mode": 2, "verify_slots": 4, "verify_block": 64, "verify_claim_min": 6},
                   {"verify_mode": 2, "verify_slots": 2, "verify_block": 32, "verify_claim_min": 32}):
-            engine.set_tuning(sid, verify_item_max=0, verify_claim_min=1, **m)
+            engine.set_tuning(sid, **dict({"verify_item_max": 0, "verify_claim_min": 1}, **m))
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
             assert list(got) == want, m
         # one item per block (the small-batch kernel)

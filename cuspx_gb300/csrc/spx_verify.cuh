@@ -66,6 +66,7 @@ struct VerifySlot {
         S_AW0, S_AW1, S_AW2,                // ADRS words 0..2 of the current layer (type WOTS)
         S_M,             // values in the current T stream (k or len)
         S_NB,            // its blocks
+        S_T0 = 15,       // slot 0 only: the warp's start time in 2^20-cycle units
         S_ROOT = 16,     // W words: the message of the current layer
         S_KEY = 24,      // 8 words: SHA-256 midstate of PUB_SEED, or PUB_SEED itself (SHAKE)
         S_LENS = 32,     // LEN bytes (17 words)
@@ -797,6 +798,10 @@ using VerifyPolicy = typename std::conditional<
     HF::kShake != 0, typename std::conditional<HF::kRobust, VerifyShakeRobust<HF>, VerifyShake<HF>>::type,
     typename std::conditional<HF::kRobust, VerifySha2Robust<HF>, VerifySha2<HF>>::type>::type;
 
+// 20 s at 2 GHz in 2^20-cycle units: far beyond any batch's run time
+// (16384 robust SHAKE-256f items take 94 ms)
+constexpr uint32_t kHyperLimitUnits = 38147;
+
 template <class HF>
 __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A, uint32_t *ctr, int G,
                                                       int claim_min) {
@@ -831,8 +836,29 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
     // always claimed at once); chains are handed out only once at least
     // claim_min lanes are free, so the claim pass runs less often
     uint32_t tpend = 0;
+    // safety net: a warp that has run longer than kHyperCycleLimit clock
+    // cycles gives up, marking its unfinished items -3 (the loop always
+    // progresses; this bounds it even so).  The start time lives in slot 0's
+    // header, in 2^20-cycle units, so it holds no register.
+    if (lane == 0) slots[PV::S_T0] = (uint32_t)(clock64() >> 20);
+    __syncwarp();
 
     while (true) {
+        if (__any_sync(0xffffffffu, (uint32_t)(clock64() >> 20) - slots[PV::S_T0] > kHyperLimitUnits)) {
+            for (int g = 0; g < G; g++) {
+                const uint32_t *S = slots + g * SW;
+                const uint32_t st = S[PV::S_STATE];
+                if (lane == 0 && (st == PV::ACTIVE || st == PV::ADVANCE)) A.verdict[S[PV::S_ITEM]] = -3;
+            }
+            while (true) {   // and every item not taken yet
+                uint32_t it = 0;
+                if (lane == 0) it = atomicAdd(ctr, 1u);
+                it = __shfl_sync(0xffffffffu, it, 0);
+                if (it >= A.count) break;
+                if (lane == 0) A.verdict[it] = -3;
+            }
+            break;
+        }
         // ---- slot upkeep: refill empty slots, set up layers (warp-uniform) ----
         for (int g = 0; upkeep && g < G; g++) {
             uint32_t *S = slots + g * SW;
@@ -940,7 +966,13 @@ __global__ void __launch_bounds__(128) k_verify_hyper(SetParams P, VerifyArgs A,
         // ---- task claims (warp-uniform; slot order is priority order, and
         // within a slot the T stream -- the critical path -- comes first) ----
         uint32_t need = __ballot_sync(0xffffffffu, kind == PV::K_NONE);
-        const bool chain_claims = __popc(need) >= claim_min;
+        // Chains are also handed out whenever no lane holds a chain or an
+        // auth-path task: the busy lanes are then T streams, which may be
+        // waiting for exactly those chains, so holding them back could stall
+        // the warp for good.  Chain and auth-path tasks always finish within
+        // a bounded number of units, so claims are never postponed for long.
+        const bool chain_claims = __popc(need) >= claim_min ||
+                                  !__any_sync(0xffffffffu, kind == PV::K_CHAIN || kind == PV::K_ROOT);
         for (uint32_t om = open & (chain_claims ? ~0u : tpend); om && need; om &= om - 1) {
             const int g = __ffs(om) - 1;
             uint32_t *S = slots + g * SW;

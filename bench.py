@@ -622,10 +622,12 @@ def served_runs(c, eng, peak_ops, peak_alu, seconds=2.0):
     names = ["sha256-128f-simple", "sha256-192f-simple", "shake256-256f-simple"]
     sids = [c.set_id(n) for n in names]
     # admission: device bytes of pending plus in-flight requests within 2 GiB,
-    # and at most 50 ms of estimated GPU work queued or in flight (requests
+    # and at most 25 ms of estimated GPU work queued or in flight (requests
     # beyond either are refused at submission); a launch carries at most
-    # 20 ms of work, so a batch of SHAKE-256-256f signs stays short
-    budget, queue_ms, launch_ms = 2 << 30, 50.0, 20.0
+    # 10 ms of work, so a batch of SHAKE-256-256f signs stays short.  At
+    # 200k req/s offered this holds the <= 64 KiB p99 to tens of ms (no
+    # limits: 150-170 ms; 50 ms / 20 ms: 50-85 ms) for ~10% fewer signs/s.
+    budget, queue_ms, launch_ms = 2 << 30, 25.0, 10.0
     srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000, mem_budget=budget, max_queue_ms=queue_ms,
                    max_launch_ms=launch_ms)
     per = 1024 // len(sids) + 1

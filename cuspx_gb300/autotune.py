@@ -10,7 +10,8 @@ bucket), and this module picks it by timing real batches on the device:
           leaf_block, fors_block, tree_warps
   verify: verify_item_max (one item per block at this size or not),
           verify_mode (layered kernels or one persistent launch), and for
-          each the chains per warp / items per warp and block size
+          each the chains per warp / items per warp, block size and the
+          persistent kernel's claim threshold
 
 Search is coordinate descent: each knob is swept with the others held, the
 best value kept, for two passes.  Every candidate is timed with CUDA events
@@ -45,6 +46,7 @@ VERIFY_SPACE = {
     "verify_slots": [2, 3, 4, 6, 8],
     "chains_per_warp": [32, 64, 128, 256, 512],
     "verify_block": [32, 64, 128],
+    "verify_claim_min": [1, 2, 3, 4],
 }
 OP_NAMES = {OP_SIGN: "sign", OP_VERIFY: "verify"}
 

@@ -288,6 +288,71 @@ SPX_DEV void keccak_f1600(uint64_t A[25]) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Keccak-f[1600] spread over one warp, for the serial sponge of a long
+// message: lane i < 25 holds state lane i (x = i % 5, y = i / 5); lanes
+// 25..31 compute values nobody reads and only take part in the shuffles.
+// A round is 20 32-bit shuffles and ~20 ALU operations on each lane instead
+// of ~190 instructions of one thread, so a permutation's latency drops
+// while a lone message is hashed.  Same function as keccak_f1600 (FIPS 202).
+// ---------------------------------------------------------------------------
+// rotation of lane i (rho, by the FIPS 202 recurrence) and the lane whose
+// rotated value lands in lane i (pi: A[x + 5y] goes to y + 5((2x + 3y) mod 5))
+__constant__ static const uint8_t KECCAK_RHO[32] = {0,  1,  62, 28, 27, 36, 44, 6,  55, 20, 3,
+                                                     10, 43, 25, 39, 41, 45, 15, 21, 8,  18, 2,
+                                                     61, 56, 14, 0,  0,  0,  0,  0,  0,  0};
+__constant__ static const uint8_t KECCAK_PI_SRC[32] = {0,  6,  12, 18, 24, 3,  9,  10, 16, 22, 1,
+                                                        7,  13, 19, 20, 4,  5,  11, 17, 23, 2,  8,
+                                                        14, 15, 21, 25, 26, 27, 28, 29, 30, 31};
+
+// per-lane constants of warp_keccak_f1600
+struct KeccakLane {
+    uint32_t col[5];      // lanes of this lane's column (C[x])
+    uint32_t xm1, xp1;    // row-0 lanes holding C[x - 1], C[x + 1]
+    uint32_t rp1, rp2;    // lanes (x + 1, y), (x + 2, y) of this row (chi)
+    uint32_t src;         // pi source lane
+    uint32_t swap, s;     // rho: halves swapped when the rotation is >= 32, then s = rotation mod 32
+};
+SPX_DEV void keccak_lane_init(KeccakLane &k, uint32_t lane) {
+    const uint32_t x = lane % 5, y = lane < 25 ? lane / 5 : 0;
+#pragma unroll
+    for (int yy = 0; yy < 5; yy++) k.col[yy] = x + 5 * yy;
+    k.xm1 = (x + 4) % 5;
+    k.xp1 = (x + 1) % 5;
+    k.rp1 = (x + 1) % 5 + 5 * y;
+    k.rp2 = (x + 2) % 5 + 5 * y;
+    k.src = KECCAK_PI_SRC[lane];
+    const uint32_t r = KECCAK_RHO[lane];
+    k.swap = r >= 32;
+    k.s = r & 31;
+}
+SPX_DEV uint64_t shfl64(uint64_t v, uint32_t src) {
+    const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
+    const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+    return ((uint64_t)hi << 32) | lo;
+}
+// every lane of the warp calls this (a: this lane's state lane)
+SPX_DEV void warp_keccak_f1600(uint64_t &a, const KeccakLane &k, uint32_t lane) {
+#pragma unroll 1
+    for (int r = 0; r < 24; r++) {
+        // theta
+        const uint64_t C = shfl64(a, k.col[0]) ^ shfl64(a, k.col[1]) ^ shfl64(a, k.col[2]) ^
+                           shfl64(a, k.col[3]) ^ shfl64(a, k.col[4]);
+        const uint64_t cp = shfl64(C, k.xp1);
+        a ^= shfl64(C, k.xm1) ^ ((cp << 1) | (cp >> 63));
+        // rho: rotate left by 32 * swap + s
+        uint32_t lo = (uint32_t)a, hi = (uint32_t)(a >> 32);
+        const uint32_t l2 = k.swap ? hi : lo, h2 = k.swap ? lo : hi;
+        lo = __funnelshift_l(h2, l2, k.s);
+        hi = __funnelshift_l(l2, h2, k.s);
+        // pi
+        const uint64_t b = shfl64(((uint64_t)hi << 32) | lo, k.src);
+        // chi + iota
+        a = b ^ (~shfl64(b, k.rp1) & shfl64(b, k.rp2));
+        if (lane == 0) a ^= KECCAK_RC[r];
+    }
+}
+
 SPX_DEV uint64_t lane_of(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
 
 // ADRS as the four little-endian Keccak lanes of its 32 bytes

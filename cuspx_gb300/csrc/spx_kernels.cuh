@@ -6,6 +6,7 @@
 // batch of thousands of signatures fills all 152 SMs:
 //
 //   k_sign_msg      thread / signature   PRF_msg, H_msg -> R, FORS digest, tree, leaf
+//   k_sign_msg_wide warp / signature     the same for messages of >= 2 KiB (SHAKE)
 //   k_sign_msg_pair 2 warps / 32 sigs    the same for messages of >= 2 KiB (SHA-256):
 //                                        schedule warp + rounds warp per message
 //   k_fors_sign     2^g lanes / FORS tree leaves (PRF+F), per-lane subtree stack,
@@ -184,7 +185,7 @@ __global__ void k_sign_msg(SetParams P, SignArgs A, uint64_t long_msg) {
     }
     const uint8_t *m = A.msg.base + A.msg.off[i];
     const uint64_t mlen = A.msg.len[i];
-    if (long_msg && mlen >= long_msg) return;   // k_sign_msg_pair hashes it
+    if (long_msg && mlen >= long_msg) return;   // k_sign_msg_pair / k_sign_msg_wide hash it
     HF::prf_msg(R, skprf, opt, m, mlen);
     uint8_t *sig = A.sig + (uint64_t)i * P.sig_bytes;
     HF::store(sig, R);
@@ -251,6 +252,63 @@ __global__ void __launch_bounds__(64) k_sign_msg_pair(SetParams P, SignArgs A, u
         HF::mgf1_digest(dg, P.dgst_bytes, st);
         A.work[i] = work_from_digest<HF>(P, dg, sk + 2 * N);
     }
+}
+
+// Long messages (SHAKE sets): one warp per message.  The sponge of
+// PRF_msg = SHAKE256(SK_PRF || optrand || m) and H_msg = SHAKE256(R || PK ||
+// m) (hash_shake256.cu:64-77, :96-130) runs with its state spread over the
+// warp (warp_keccak_f1600): lane j < 17 loads and absorbs stream lane j of
+// each 136-byte block (one coalesced 136-byte read per block, fetched a
+// block ahead), and the prefix -- 2n or 3n bytes, whole lanes -- sits in
+// lanes below 17 of the first block.  A 1 MiB message is 7,711 serial
+// permutations per pass, so a permutation's latency is the message's.
+// every lane: stream = prefix (P lanes; lane j < P holds lane j) || m || padding
+template <class HF>
+SPX_DEV void shake_absorb_warp(uint64_t &a, const KeccakLane &k, uint32_t lane, uint64_t pre, int P,
+                               const uint8_t *m, uint64_t mlen) {
+    const uint64_t nblocks = (8 * (uint64_t)P + mlen) / 136 + 1;
+    auto block_lane = [&](uint64_t b) -> uint64_t {
+        const uint64_t q = 17 * b + lane;
+        if (lane >= 17) return 0ull;
+        if (q < (uint64_t)P) return pre;
+        return HF::msg_lane(m, mlen, q - P);   // the 0x1F padding byte included
+    };
+    a = 0;
+    uint64_t nxt = block_lane(0);
+    for (uint64_t b = 0; b < nblocks; b++) {
+        uint64_t cur = nxt;
+        if (b + 1 < nblocks) nxt = block_lane(b + 1);
+        if (b + 1 == nblocks && lane == 16) cur ^= 0x8000000000000000ull;
+        a ^= cur;
+        warp_keccak_f1600(a, k, lane);
+    }
+}
+
+template <class HF>
+__global__ void __launch_bounds__(128) k_sign_msg_wide(SetParams P, SignArgs A, uint64_t long_msg) {
+    constexpr int N = 4 * HF::W, NL = N / 8;
+    __shared__ uint64_t dgs[4][8];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t i = blockIdx.x * 4 + wib;
+    if (i >= A.count) return;                 // warp-uniform
+    const uint64_t mlen = A.msg.len[i];
+    if (mlen < long_msg) return;              // k_sign_msg hashes it
+    KeccakLane k;
+    keccak_lane_init(k, lane);
+    const uint8_t *sk = A.sk.row(i);
+    const uint8_t *m = A.msg.base + A.msg.off[i];
+    uint64_t pre = 0, a;
+    if (lane < NL) pre = reinterpret_cast<const uint64_t *>(sk + N)[lane];
+    else if (lane < 2 * NL)
+        pre = A.optrand ? reinterpret_cast<const uint64_t *>(A.optrand + (uint64_t)i * N)[lane - NL]
+                        : 0xadadadadadadadadull;   // the reference's fixed optrand (sign.cu:1950-1954)
+    shake_absorb_warp<HF>(a, k, lane, pre, 2 * NL, m, mlen);
+    if (lane < NL) reinterpret_cast<uint64_t *>(A.sig + (uint64_t)i * P.sig_bytes)[lane] = a;   // R
+    pre = lane < NL ? a : (lane < 3 * NL ? reinterpret_cast<const uint64_t *>(sk + 2 * N)[lane - NL] : 0ull);
+    shake_absorb_warp<HF>(a, k, lane, pre, 3 * NL, m, mlen);
+    if (lane < 8) dgs[wib][lane] = a;
+    __syncwarp();
+    if (lane == 0) A.work[i] = work_from_digest<HF>(P, reinterpret_cast<const uint8_t *>(dgs[wib]), sk + 2 * N);
 }
 
 // ===========================================================================
@@ -765,7 +823,7 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A, uint64_t long_msg) {
         A.work[i] = w;
         return;
     }
-    if (long_msg && A.msg.len[i] >= long_msg) return;   // k_verify_msg_pair hashes it
+    if (long_msg && A.msg.len[i] >= long_msg) return;   // k_verify_msg_pair / _wide hash it
     const uint8_t *pkb = A.pk.row(i);
     const uint8_t *sig = A.sig + (uint64_t)i * A.sig_stride;
     uint32_t R[W], pk[2 * W];
@@ -813,6 +871,31 @@ __global__ void __launch_bounds__(64) k_verify_msg_pair(SetParams P, VerifyArgs 
         HF::mgf1_digest(dg, P.dgst_bytes, st);
         A.work[i] = work_from_digest<HF>(P, dg, pkb);
     }
+}
+
+// H_msg of long messages (SHAKE sets): one warp per message, as in
+// k_sign_msg_wide
+template <class HF>
+__global__ void __launch_bounds__(128) k_verify_msg_wide(SetParams P, VerifyArgs A, uint64_t long_msg) {
+    constexpr int N = 4 * HF::W, NL = N / 8;
+    __shared__ uint64_t dgs[4][8];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t i = blockIdx.x * 4 + wib;
+    if (i >= A.count) return;                                           // warp-uniform
+    if (A.siglen && A.siglen[i] != (uint64_t)P.sig_bytes) return;      // rejected by k_verify_msg
+    const uint64_t mlen = A.msg.len[i];
+    if (mlen < long_msg) return;                                        // k_verify_msg hashes it
+    KeccakLane k;
+    keccak_lane_init(k, lane);
+    const uint8_t *pkb = A.pk.row(i);
+    const uint8_t *sig = A.sig + (uint64_t)i * A.sig_stride;
+    uint64_t a;
+    const uint64_t pre = lane < NL ? reinterpret_cast<const uint64_t *>(sig)[lane]
+                                   : (lane < 3 * NL ? reinterpret_cast<const uint64_t *>(pkb)[lane - NL] : 0ull);
+    shake_absorb_warp<HF>(a, k, lane, pre, 3 * NL, A.msg.base + A.msg.off[i], mlen);
+    if (lane < 8) dgs[wib][lane] = a;
+    __syncwarp();
+    if (lane == 0) A.work[i] = work_from_digest<HF>(P, reinterpret_cast<const uint8_t *>(dgs[wib]), pkb);
 }
 
 // root from a leaf and its auth path (compute_root, utils.cu:94-135)

@@ -150,6 +150,9 @@ struct Family {
         if constexpr (!HF::kShake) {
             if ((e = cudaFuncGetAttributes(&fa, (const void *)k_sign_msg_pair<HF>))) return e;
             if ((e = cudaFuncGetAttributes(&fa, (const void *)k_verify_msg_pair<HF>))) return e;
+        } else {
+            if ((e = cudaFuncGetAttributes(&fa, (const void *)k_sign_msg_wide<HF>))) return e;
+            if ((e = cudaFuncGetAttributes(&fa, (const void *)k_verify_msg_wide<HF>))) return e;
         }
         return cudaSuccess;
     }
@@ -224,13 +227,15 @@ struct Family {
     static void sign(const SetParams &P, const SignArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
                      uint64_t long_msg, const StreamFork *fk) {
         if (A.count == 0) return;
-        if (HF::kShake) long_msg = 0;   // the two-warp message kernels are SHA-256 only
         k_sign_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A, long_msg);
         CUSPX_MARK(pt, "k_sign_msg", s);
-        if constexpr (!HF::kShake) {
-            if (long_msg) {
+        if (long_msg) {   // messages of >= long_msg bytes: two warps per 32 (SHA-256), a warp each (SHAKE)
+            if constexpr (!HF::kShake) {
                 k_sign_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A, long_msg);
                 CUSPX_MARK(pt, "k_sign_msg_pair", s);
+            } else {
+                k_sign_msg_wide<HF><<<ceil_div(A.count, 4), 128, 0, s>>>(P, A, long_msg);
+                CUSPX_MARK(pt, "k_sign_msg_wide", s);
             }
         }
         const bool split = fk && !pt;
@@ -268,13 +273,15 @@ struct Family {
     static void verify(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
                        uint64_t long_msg) {
         if (A.count == 0) return;
-        if (HF::kShake) long_msg = 0;
         k_verify_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A, long_msg);
         CUSPX_MARK(pt, "k_verify_msg", s);
-        if constexpr (!HF::kShake) {
-            if (long_msg) {
+        if (long_msg) {
+            if constexpr (!HF::kShake) {
                 k_verify_msg_pair<HF><<<ceil_div(A.count, 32), 64, 0, s>>>(P, A, long_msg);
                 CUSPX_MARK(pt, "k_verify_msg_pair", s);
+            } else {
+                k_verify_msg_wide<HF><<<ceil_div(A.count, 4), 128, 0, s>>>(P, A, long_msg);
+                CUSPX_MARK(pt, "k_verify_msg_wide", s);
             }
         }
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);

@@ -413,3 +413,37 @@ def test_null_message_slab_is_refused(engine):
         rc = engine.L.cuspx_verify_batch(engine.h, sid, 1, bytes(32), None, off.ctypes.data, lens.ctypes.data,
                                          sig, None, v.ctypes.data)
         assert rc == (-1 if ln else 0), ln
+
+
+@pytest.mark.parametrize("setname", ["shake256-128f-simple", "shake256-256f-simple", "shake256-192f-robust"])
+def test_long_messages_warp_sponge(engine, setname):
+    """SHAKE messages of 2 KiB and more are hashed one warp per message (the
+    sponge state spread over the lanes); signatures and verdicts equal the
+    oracle's on both sides of the threshold and on every 136-byte block edge
+    of PRF_msg (prefix 2n bytes) and H_msg (prefix 3n bytes), with a
+    corrupted and a wrong-length signature mixed in."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    n = o.p.n
+    rng = random.Random(136)
+    seed = bytes(rng.randrange(256) for _ in range(3 * n))
+    pk, sk = o.seed_keypair(seed)
+    lens = [0, 100, 2047, 2048, 2049]
+    for pre in (2 * n, 3 * n):
+        for d in (-2, -1, 0, 1):
+            lens.append(136 * 16 - pre + d)   # the padding byte at a block's last byte, or a new block
+    lens += [20000, 64]
+    msgs = [rng.randbytes(L) for L in lens]
+    sigs, st = engine.sign_batch(sid, [sk] * len(msgs), msgs)
+    assert list(st) == [0] * len(msgs)
+    for m, s in zip(msgs, sigs):
+        assert s == o.sign(m, sk), len(m)
+    bad = bytearray(sigs[-2])
+    bad[rng.randrange(len(bad))] ^= 0x10
+    vsigs = list(sigs) + [bytes(bad), sigs[4]]
+    vmsgs = msgs + [msgs[-2], msgs[4]]
+    siglens = [len(s) for s in vsigs[:-1]] + [len(sigs[4]) - 1]
+    want = [o.verify(s, m, pk) for s, m in zip(vsigs[:-1], vmsgs[:-1])] + [-1]
+    assert want.count(-1) == 2
+    got = engine.verify_batch(sid, [pk] * len(vmsgs), vmsgs, vsigs, siglens=siglens)
+    assert list(got) == want

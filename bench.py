@@ -626,7 +626,8 @@ def served_runs(c, eng, peak_ops, peak_alu, seconds=2.0):
     # beyond either are refused at submission); a launch carries at most
     # 10 ms of work, so a batch of SHAKE-256-256f signs stays short.  At
     # 200k req/s offered this holds the <= 64 KiB p99 to tens of ms (no
-    # limits: 150-170 ms; 50 ms / 20 ms: 50-85 ms) for ~10% fewer signs/s.
+    # limits: 150-170 ms; 50 ms / 20 ms: 50-85 ms), at the price of smaller
+    # launches: ~25% fewer signs/s at saturation, verifies/s unchanged.
     budget, queue_ms, launch_ms = 2 << 30, 25.0, 10.0
     srv = c.Server(eng, max_batch=1024, max_inflight=3, window_us=1000, mem_budget=budget, max_queue_ms=queue_ms,
                    max_launch_ms=launch_ms)

@@ -9,9 +9,10 @@ bucket), and this module picks it by timing real batches on the device:
           size), fors_lanes_log2 (lanes per FORS tree), tree_mode,
           leaf_block, fors_block, tree_warps
   verify: verify_item_max (one item per block at this size or not),
-          verify_mode (layered kernels or one persistent launch), and for
-          each the chains per warp / items per warp, block size and the
-          persistent kernel's claim threshold
+          verify_mode (layered kernels, one persistent launch, or layered
+          kernels over length-sorted chains), and for each the chains per
+          warp / items per warp, block size, the persistent kernel's claim
+          threshold and the sorted mode's item groups
 
 Search is coordinate descent: each knob is swept with the others held, the
 best value kept, for two passes.  Every candidate is timed with CUDA events
@@ -42,11 +43,13 @@ SIGN_SPACE = {
 }
 VERIFY_SPACE = {
     "verify_item_max": [0, None],   # None: this bucket's size (one item per block)
-    "verify_mode": [0, 1, 2],
+    "verify_sorted_min": [0, 1],    # 1: every batch of this bucket verifies as verify_mode 3
+    "verify_mode": [0, 1, 2, 3],
     "verify_slots": [2, 3, 4, 6, 8],
     "chains_per_warp": [32, 64, 128, 256, 512],
     "verify_block": [32, 64, 128],
     "verify_claim_min": [1, 2, 3, 4],
+    "verify_groups": [2, 4, 6, 8],
 }
 OP_NAMES = {OP_SIGN: "sign", OP_VERIFY: "verify"}
 

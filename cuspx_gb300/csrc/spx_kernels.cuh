@@ -921,13 +921,14 @@ SPX_DEV void compute_root(uint32_t root[HF::W], const uint32_t leaf[HF::W], uint
     for (int x = 0; x < W; x++) root[x] = cur[x];
 }
 
-// FORS roots from the signature: thread per (item, tree) (fors_pk_from_sig, fors.cu:596-631)
+// FORS roots from the signature: thread per (item, tree) of items
+// [first, first + n) (fors_pk_from_sig, fors.cu:596-631)
 template <class HF>
-__global__ void k_verify_fors(SetParams P, VerifyArgs A) {
+__global__ void k_verify_fors(SetParams P, VerifyArgs A, uint32_t first, uint32_t n) {
     constexpr int W = HF::W, N = 4 * W;
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (uint64_t)A.count * P.k) return;
-    const uint32_t item = (uint32_t)(gid / P.k);
+    if (gid >= (uint64_t)n * P.k) return;
+    const uint32_t item = first + (uint32_t)(gid / P.k);
     const int t = (int)(gid % P.k);
     const SignWork wk = A.work[item];
     if (wk.flags) return;
@@ -1039,9 +1040,65 @@ __global__ void k_verify_ht(SetParams P, VerifyArgs A) {
 //                    with L = -1 it computes the FORS key T_k instead, and at
 //                    L = d-1 it compares with PK.root (sign.cu:3116)
 // ---------------------------------------------------------------------------
+// Root of layer L of an item into root[]: L = -1 the FORS key T_k over the
+// k FORS roots at `vals`; otherwise T_len over the len WOTS+ public-key
+// values at `vals`, then the subtree root from the auth path at `auth`.  The
+// values and the auth path may sit in global or shared memory.  tb: the
+// thread's T stream scratch of HF::kSmemWords shared words.
+template <class HF>
+SPX_DEV void verify_layer_root(const SetParams &P, const SignWork &wk, const KeyRegs<4 * HF::W> &key, int L,
+                               uint32_t *tb, const uint8_t *vals, const uint8_t *auth, uint32_t root[HF::W]) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    typename HF::TStream ts;
+    if (L < 0) {
+        Adrs pa;
+        adrs_zero(pa);
+        adrs_tree(pa, wk.tree);
+        adrs_keypair(pa, wk.idx_leaf);
+        adrs_type(pa, ADDR_FORSPK);
+        HF::t_init(ts, tb, key, pa);
+        for (int t = 0; t < P.k; t++) {
+            uint32_t v[W];
+            HF::load(v, vals + (uint64_t)t * N);
+            HF::t_absorb(ts, v, key);
+        }
+        HF::t_final(root, ts);
+        return;
+    }
+    uint64_t tree_L;
+    uint32_t idx_L;
+    layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    Adrs pa;
+    adrs_zero(pa);
+    adrs_layer(pa, L);
+    adrs_tree(pa, tree_L);
+    adrs_keypair(pa, idx_L);
+    adrs_type(pa, ADDR_WOTSPK);
+    HF::t_init(ts, tb, key, pa);
+    for (int c = 0; c < LEN; c++) {
+        uint32_t v[W];
+        HF::load(v, vals + (uint64_t)c * N);
+        HF::t_absorb(ts, v, key);
+    }
+    uint32_t leaf[W];
+    HF::t_final(leaf, ts);
+    Adrs ta;
+    adrs_zero(ta);
+    adrs_layer(ta, L);
+    adrs_tree(ta, tree_L);
+    adrs_type(ta, ADDR_HASHTREE);
+    compute_root<HF>(root, leaf, idx_L, 0, auth, P.hp, ta, key);
+}
+
+// offset of layer L's WOTS+ signature in a signature (sign.cu:3092-3110);
+// its auth path follows at + wots_bytes
+SPX_DEV uint64_t sig_layer_off(const SetParams &P, int L) {
+    return (uint64_t)P.n + P.fors_bytes + (uint64_t)L * (P.wots_bytes + (uint64_t)P.hp * P.n);
+}
+
 template <class HF>
 __global__ void k_verify_root(SetParams P, VerifyArgs A, int L) {
-    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    constexpr int W = HF::W, N = 4 * W;
     extern __shared__ uint32_t smem[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.count) return;
@@ -1053,50 +1110,11 @@ __global__ void k_verify_root(SetParams P, VerifyArgs A, int L) {
     const uint8_t *pkb = A.pk.row(i);
     KeyRegs<N> key;
     key_from_work<HF>(key, pkb, pkb, wk);
-    uint32_t *tb = smem + threadIdx.x * HF::kSmemWords;
+    constexpr int LEN = 2 * N + 3;
+    const uint8_t *vals = L < 0 ? A.fors_roots + (uint64_t)i * P.k * N : A.wpk + (uint64_t)i * LEN * N;
+    const uint8_t *auth = A.sig + (uint64_t)i * A.sig_stride + (L < 0 ? 0 : sig_layer_off(P, L) + P.wots_bytes);
     uint32_t root[W];
-    typename HF::TStream ts;
-    if (L < 0) {
-        Adrs pa;
-        adrs_zero(pa);
-        adrs_tree(pa, wk.tree);
-        adrs_keypair(pa, wk.idx_leaf);
-        adrs_type(pa, ADDR_FORSPK);
-        HF::t_init(ts, tb, key, pa);
-        for (int t = 0; t < P.k; t++) {
-            uint32_t v[W];
-            HF::load(v, A.fors_roots + ((uint64_t)i * P.k + t) * N);
-            HF::t_absorb(ts, v, key);
-        }
-        HF::t_final(root, ts);
-    } else {
-        uint64_t tree_L;
-        uint32_t idx_L;
-        layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
-        Adrs pa;
-        adrs_zero(pa);
-        adrs_layer(pa, L);
-        adrs_tree(pa, tree_L);
-        adrs_keypair(pa, idx_L);
-        adrs_type(pa, ADDR_WOTSPK);
-        HF::t_init(ts, tb, key, pa);
-        const uint8_t *wp = A.wpk + (uint64_t)i * LEN * N;
-        for (int c = 0; c < LEN; c++) {
-            uint32_t v[W];
-            HF::load(v, wp + (uint64_t)c * N);
-            HF::t_absorb(ts, v, key);
-        }
-        uint32_t leaf[W];
-        HF::t_final(leaf, ts);
-        Adrs ta;
-        adrs_zero(ta);
-        adrs_layer(ta, L);
-        adrs_tree(ta, tree_L);
-        adrs_type(ta, ADDR_HASHTREE);
-        const uint8_t *auth = A.sig + (uint64_t)i * A.sig_stride + N + P.fors_bytes +
-                              (uint64_t)L * (P.wots_bytes + P.hp * N) + P.wots_bytes;
-        compute_root<HF>(root, leaf, idx_L, 0, auth, P.hp, ta, key);
-    }
+    verify_layer_root<HF>(P, wk, key, L, smem + threadIdx.x * HF::kSmemWords, vals, auth, root);
     if (L == P.d - 1) {
         uint32_t pr[W];
         HF::load(pr, pkb + N);

@@ -10,6 +10,7 @@
 
 #include "spx_kernels.cuh"
 #include "spx_verify.cuh"
+#include "spx_vsort.cuh"
 
 namespace cuspx {
 
@@ -21,13 +22,15 @@ struct Tuning {
     int tree_warps = 4;      // warps per block for k_trees (upper bound)
     int chains_per_warp = 64;  // (item, chain) tasks per warp in k_verify_chains
     int verify_mode = 0;     // 0 layered kernels, 1 one thread per item over all layers,
-                             // 2 persistent hypertree kernel
+                             // 2 persistent hypertree kernel, 3 layered with sorted chains
     int fors_lanes_log2 = 5; // lanes per FORS tree = 2^g (0: lane per tree, 5: warp per tree)
     int tree_mode = 0;       // 0 warp per XMSS tree, 1 lane per tree (subtrees of height <= 4)
     int chain_mode_max = 64; // batches of at most this many items run XMSS leaves chain-parallel
     int verify_slots = 4;    // most items per warp in the persistent verify kernel
     int verify_item_max = 0; // batches of at most this many items verify one item per block
     int verify_claim_min = 1;// persistent verify: free lanes before chains are handed out
+    int verify_groups = 4;   // sorted verify: item groups on their own streams (1..8)
+    int verify_sorted_min = 0; // batches of at least this many items verify as verify_mode 3 (0: never by size)
 };
 
 struct KeygenArgs {
@@ -70,6 +73,16 @@ struct StreamFork {
     cudaEvent_t fork, join;
 };
 
+// Streams of a verify batch for verify_mode 3: group g > 0 runs on side[g-1]
+// between `fork` and join[g-1]; chain[g] orders group g+1's chain kernel of a
+// layer after group g's.  Works inside graph capture.
+struct VerifyFork {
+    static constexpr int kMaxGroups = 8;
+    int sides = 0;   // side streams available (groups beyond sides + 1 are not used)
+    cudaStream_t side[kMaxGroups - 1] = {};
+    cudaEvent_t fork = nullptr, join[kMaxGroups - 1] = {}, chain[kMaxGroups - 1] = {};
+};
+
 struct FamilyOps {
     cudaError_t (*configure)();
     // long_msg: messages of at least this many bytes are hashed two warps per
@@ -77,8 +90,10 @@ struct FamilyOps {
     // fk: optional side stream (ignored while per-kernel timing is on).
     void (*sign)(const SetParams &, const SignArgs &, const Tuning &, cudaStream_t, PhaseTimer *, uint64_t long_msg,
                  const StreamFork *fk);
+    // vl / vf: bucket lists and streams of verify_mode 3 (null: that mode
+    // runs as verify_mode 2)
     void (*verify)(const SetParams &, const VerifyArgs &, const Tuning &, cudaStream_t, PhaseTimer *,
-                   uint64_t long_msg);
+                   uint64_t long_msg, const VerifyLists *vl, const VerifyFork *vf);
     void (*keygen)(const SetParams &, const KeygenArgs &, const Tuning &, cudaStream_t, PhaseTimer *);
     int smem_words;    // per-thread T_l stream scratch
 };
@@ -136,6 +151,7 @@ struct Family {
             if ((e = cudaFuncSetAttribute(k_verify_hyper<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big)))
                 return e;
         if ((e = cudaFuncSetAttribute(k_verify_item<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_vsort_layer<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         // Load every other kernel of the family now: with lazy module loading
         // a kernel's first launch loads it, and in a server that first launch
         // is a request's (one took ~50 ms of host time and held back every
@@ -144,7 +160,8 @@ struct Family {
         const void *rest[] = {(const void *)k_sign_msg<HF>, (const void *)k_leaf_chains<HF>,
                               (const void *)k_trees_lane<HF>, (const void *)k_sign_finish<HF>,
                               (const void *)k_verify_msg<HF>, (const void *)k_verify_fors<HF>,
-                              (const void *)k_verify_chains<HF>, (const void *)k_keygen_finish<N>};
+                              (const void *)k_verify_chains<HF>, (const void *)k_vsort_chains<HF>,
+                              (const void *)k_keygen_finish<N>};
         for (const void *f : rest)
             if ((e = cudaFuncGetAttributes(&fa, f))) return e;
         if constexpr (!HF::kShake) {
@@ -270,8 +287,63 @@ struct Family {
         CUSPX_MARK(pt, "k_sign_finish", s);
     }
 
+    static constexpr uint32_t kLayerSmem = 200u * 1024u;   // the shared-memory limit configure() sets
+
+    // verify_mode 3: per group of items, T_k then per layer the sorted
+    // chains and the layer roots (spx_vsort.cuh).  Groups run on their own
+    // streams; a group's chain kernel of layer L starts after the previous
+    // group's, so the groups keep an offset and one group's serial layer
+    // kernel overlaps the next group's chains.  With per-kernel timing on
+    // every group runs on s.
+    static void verify_sorted(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s,
+                              PhaseTimer *pt, const VerifyLists &V, const VerifyFork *vf) {
+        constexpr int LEN = 2 * N + 3;
+        int G = tu.verify_groups < 1 ? 1 : tu.verify_groups;
+        const int gmax = pt || !vf ? 1 : vf->sides + 1;
+        if (G > gmax) G = gmax;
+        if ((uint32_t)G > A.count) G = (int)A.count;
+        const uint32_t per = (A.count + G - 1) / G;
+        G = (int)((A.count + per - 1) / per);
+        // thread per item in the layer kernel, whose slots must fit the
+        // 200 KiB of shared memory configured for it (32 threads fit for
+        // every set: SHAKE-256f-robust needs 176 KiB)
+        int b = tu.verify_block;
+        while (b > 32 && VsortSmem<HF>::bytes(P, (uint32_t)b) > kLayerSmem) b /= 2;
+        const size_t smem = VsortSmem<HF>::bytes(P, (uint32_t)b);
+        cudaMemsetAsync(V.cnt, 0, (size_t)G * P.d * 16 * sizeof(uint32_t), s);
+        cudaStream_t gs[VerifyFork::kMaxGroups];
+        gs[0] = s;
+        if (G > 1) cudaEventRecord(vf->fork, s);
+        for (int g = 1; g < G; g++) {
+            gs[g] = vf->side[g - 1];
+            cudaStreamWaitEvent(gs[g], vf->fork, 0);
+        }
+        auto first = [&](int g) { return (uint32_t)g * per; };
+        auto items = [&](int g) { return g + 1 < G ? per : A.count - (uint32_t)g * per; };
+        for (int g = 0; g < G; g++) {
+            k_verify_fors<HF><<<ceil_div((uint64_t)items(g) * P.k, 128), 128, 0, gs[g]>>>(P, A, first(g), items(g));
+            CUSPX_MARK(pt, "k_verify_fors", s);
+            k_vsort_layer<HF><<<ceil_div(items(g), b), b, smem, gs[g]>>>(P, A, V, -1, first(g), items(g), g);
+            CUSPX_MARK(pt, "k_vsort_layer", s);
+        }
+        for (int L = 0; L < P.d; L++) {
+            for (int g = 0; g < G; g++) {
+                if (g > 0) cudaStreamWaitEvent(gs[g], vf->chain[g - 1], 0);
+                k_vsort_chains<HF><<<ceil_div((uint64_t)items(g) * LEN, 128), 128, 0, gs[g]>>>(P, A, V, L, first(g), g);
+                CUSPX_MARK(pt, "k_vsort_chains", s);
+                if (g + 1 < G) cudaEventRecord(vf->chain[g], gs[g]);
+                k_vsort_layer<HF><<<ceil_div(items(g), b), b, smem, gs[g]>>>(P, A, V, L, first(g), items(g), g);
+                CUSPX_MARK(pt, "k_vsort_layer", s);
+            }
+        }
+        for (int g = 1; g < G; g++) {
+            cudaEventRecord(vf->join[g - 1], gs[g]);
+            cudaStreamWaitEvent(s, vf->join[g - 1], 0);
+        }
+    }
+
     static void verify(const SetParams &P, const VerifyArgs &A, const Tuning &tu, cudaStream_t s, PhaseTimer *pt,
-                       uint64_t long_msg) {
+                       uint64_t long_msg, const VerifyLists *vl, const VerifyFork *vf) {
         if (A.count == 0) return;
         k_verify_msg<HF><<<ceil_div(A.count, 128), 128, 0, s>>>(P, A, long_msg);
         CUSPX_MARK(pt, "k_verify_msg", s);
@@ -284,7 +356,16 @@ struct Family {
                 CUSPX_MARK(pt, "k_verify_msg_wide", s);
             }
         }
-        k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A);
+        const bool want_sorted =
+            tu.verify_mode == 3 || (tu.verify_sorted_min > 0 && A.count >= (uint32_t)tu.verify_sorted_min);
+        const bool sorted = want_sorted && vl && vl->tasks && vl->stride >= (uint64_t)A.count * (2 * N + 3) &&
+                            A.count < (1u << 25) && VsortSmem<HF>::bytes(P, 32) <= kLayerSmem && P.len1 == 2 * N &&
+                            P.len2 == 3 && !(tu.verify_item_max > 0 && A.count <= (uint32_t)tu.verify_item_max);
+        if (sorted) {   // FORS per item group, beside the other groups' layers
+            verify_sorted(P, A, tu, s, pt, *vl, vf);
+            return;
+        }
+        k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A, 0, A.count);
         CUSPX_MARK(pt, "k_verify_fors", s);
         if (tu.verify_item_max > 0 && A.count <= (uint32_t)tu.verify_item_max && P.hp <= 9) {
             // small batches: one item per block (its serial path sets the time)
@@ -296,7 +377,7 @@ struct Family {
             return;
         }
         const int b = tu.verify_block;
-        if (tu.verify_mode == 2 && kPersistVerify && A.ctr && P.hp <= 9) {
+        if (tu.verify_mode >= 2 && kPersistVerify && A.ctr && P.hp <= 9) {
             verify_persistent(P, A, tu, s, pt);
             return;
         }

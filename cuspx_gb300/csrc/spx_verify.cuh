@@ -138,16 +138,17 @@ struct VerifySha2 : VerifySlot<4 * HF::W, 22, 64> {
 #pragma unroll
         for (int i = 0; i < W; i++) v[i] = __byte_perm(stream[w0 + i], stream[w0 + i + 1], 0x2345);
     }
+    // value bytes 8q .. 8q+7 (memory order) to stream byte 22 + 8q
+    SPX_DEV static void put_value_word(uint32_t *stream, int q, uint2 x) {
+        const int o = 22 + 8 * q;
+        put16(stream, o, x.x);
+        stream[(o + 2) / 4] = __byte_perm(x.x, x.y, 0x5432);
+        put16(stream, o + 6, x.y >> 16);
+    }
     // `bytes` (multiple of 8) from 8-byte aligned global memory to stream
     // byte 22 onwards, warp-cooperatively
     SPX_DEV static void copy_values(uint32_t *stream, const uint8_t *src, int bytes, uint32_t lane) {
-        for (int q = lane; q < bytes / 8; q += 32) {
-            const uint2 x = reinterpret_cast<const uint2 *>(src)[q];
-            const int o = 22 + 8 * q;
-            put16(stream, o, x.x);
-            stream[(o + 2) / 4] = __byte_perm(x.x, x.y, 0x5432);
-            put16(stream, o + 6, x.y >> 16);
-        }
+        for (int q = lane; q < bytes / 8; q += 32) put_value_word(stream, q, reinterpret_cast<const uint2 *>(src)[q]);
     }
     // ADRS_c prefix and the padding after m values (the length counts the
     // 64-byte midstate block)
@@ -313,6 +314,10 @@ struct VerifyShake : VerifySlot<4 * HF::W, 4 * HF::W + 32, 136> {
         const uint32_t *s = stream + 2 * (kPreLanes + c * NL);
 #pragma unroll
         for (int i = 0; i < W; i++) v[i] = s[i];
+    }
+    // value bytes 8q .. 8q+7 (memory order) to value lane q
+    SPX_DEV static void put_value_word(uint32_t *stream, int q, uint2 x) {
+        lanes(stream)[kPreLanes + q] = (uint64_t)x.y << 32 | x.x;
     }
     SPX_DEV static void copy_values(uint32_t *stream, const uint8_t *src, int bytes, uint32_t lane) {
         uint64_t *d = lanes(stream) + kPreLanes;

@@ -1,0 +1,307 @@
+// spx_vsort.cuh -- layered verify with the WOTS+ chains sorted by length.
+//
+// crypto_sign_verify (sign.cu:3048-3121) is serial over the d layers of an
+// item, and per layer a WOTS+ chain c runs 15 - d_c steps of F
+// (wots_pk_from_sig, wots.cu:777-804) where d_c is digit c of the layer's
+// message (chain_lengths, wots.cu:84-166): 0 to 15 steps, 7.5 on average.
+// A warp that runs 32 chains of mixed lengths side by side is busy for the
+// longest of them, so half its lanes idle on average.
+//
+// Here each layer's chains are bucketed by their number of steps when the
+// layer's message becomes known, and the chain kernel hands sorted positions
+// to lanes in order: the 32 lanes of a warp hold chains of one length
+// (two lengths at a bucket edge), no lane idles and nothing is claimed
+// inside the loop.  Buckets are enumerated longest first, so the longest
+// chains start in the first blocks the GPU schedules.
+//
+// Per group of items the launch sequence is
+//
+//   k_vsort_layer(L = -1)    T_k over the FORS roots; bucket layer 0's chains
+//   k_vsort_chains(L = 0)    every chain of layer 0
+//   k_vsort_layer(L = 0)     T_len, auth path -> root; bucket layer 1's chains
+//   ...
+//   k_vsort_layer(L = d-1)   T_len, auth path -> root; compare with PK.root
+//
+// k_vsort_layer is one thread per item and spends its time in a serial chain
+// of ~13 compressions (T_len and the auth path), so the host splits the
+// batch into groups on separate streams: one group's layer kernel runs while
+// another group's chain kernel keeps the ALU pipes full.
+//
+// A chain of zero steps is its signature value: it sorts last, and its lane
+// in the chain kernel copies the value to the WOTS+ public key buffer.
+#pragma once
+#include "spx_verify.cuh"
+
+#define SPX_HD __host__ __device__ __forceinline__
+
+namespace cuspx {
+
+// Chains of each layer bucketed by steps (0..15).  Bucket l holds up to
+// `stride` 32-bit entries item << 7 | chain; group g uses entries
+// [first_g x len, (first_g + items_g) x len) of every bucket and counters
+// cnt[(g x d + L) x 16 + l].
+struct VerifyLists {
+    uint32_t *tasks = nullptr;   // 16 x stride entries
+    uint32_t *cnt = nullptr;     // groups x d x 16 counters, zeroed before the first group starts
+    uint64_t stride = 0;         // entries per bucket: at least count x len
+};
+
+// steps of WOTS+ chain c for message msg: 15 - digit c (chain_lengths,
+// wots.cu:84-166; w = 16 in every set, so len1 = 2n and len2 = 3); csum is
+// the shifted checksum from vsort_checksum.  Called with constant c only
+// (unrolled loops), so msg stays in registers.
+template <class HF>
+SPX_DEV uint32_t vsort_steps(const uint32_t msg[HF::W], uint32_t csum, int c) {
+    constexpr int LEN1 = 8 * HF::W, LEN2 = 3;
+    uint32_t d;
+    if (c < LEN1) {
+        uint32_t byte;
+        if (HF::kShake) byte = (msg[c >> 3] >> (8 * ((c >> 1) & 3))) & 0xffu;
+        else byte = (msg[c >> 3] >> (24 - 8 * ((c >> 1) & 3))) & 0xffu;
+        d = (c & 1) ? (byte & 15u) : (byte >> 4);
+    } else {
+        constexpr int cbits = ((LEN2 * 4 + 7) / 8) * 8;
+        d = (csum >> (cbits - 4 * (c - LEN1 + 1))) & 15u;
+    }
+    return 15u - d;
+}
+template <class HF>
+SPX_DEV uint32_t vsort_checksum(const uint32_t msg[HF::W]) {
+    constexpr int LEN1 = 8 * HF::W, LEN2 = 3;
+    uint32_t csum = 0;
+#pragma unroll
+    for (int c = 0; c < LEN1; c++) csum += vsort_steps<HF>(msg, 0, c);
+    return csum << ((8 - ((LEN2 * 4) % 8)) % 8);
+}
+
+// Dynamic shared memory of k_vsort_layer for blocks of b threads: a verify
+// slot per thread (spx_verify.cuh: the T input stream in memory byte order,
+// the auth path, key material and, for robust sets, the T mask stream), then
+// per thread its chains' buckets and ranks for the next layer.
+template <class HF>
+struct VsortSmem {
+    using PV = VerifyPolicy<HF>;
+    SPX_HD static uint32_t slot_stride(int hp) { return ((uint32_t)PV::slot_words(hp) + 3u) & ~3u; }
+    SPX_HD static uint32_t lr_off(const SetParams &P, uint32_t b) { return b * slot_stride(P.hp) * 4u; }
+    SPX_HD static uint32_t bytes(const SetParams &P, uint32_t b) { return lr_off(P, b) + b * (uint32_t)PV::LEN * 4u; }
+};
+
+// Thread per item of the group [first, first + n): the root of layer L (T_k
+// for L = -1), then either the verdict (L = d-1) or layer L+1's chains
+// bucketed by steps.  The block stages its items' values and auth paths into
+// their slots with coalesced copies first; each thread then runs its item's
+// T stream and auth path unit by unit through the verify policy (one hash
+// call site per loop, so a warp running alone on its SM keeps the code in
+// its instruction cache).  Dynamic shared memory: VsortSmem<HF>::bytes.
+template <class HF>
+__global__ void k_vsort_layer(SetParams P, VerifyArgs A, VerifyLists V, int L, uint32_t first, uint32_t n,
+                              int grp) {
+    using PV = VerifyPolicy<HF>;
+    using SM = VsortSmem<HF>;
+    constexpr int W = PV::W, N = PV::N, LEN = PV::LEN;
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint32_t hcount[16], hbase[16];
+    if (threadIdx.x < 16) hcount[threadIdx.x] = 0;
+    const uint32_t stride = SM::slot_stride(P.hp);
+    const uint32_t j0 = blockIdx.x * blockDim.x;
+    const uint32_t nb = n - j0 < blockDim.x ? n - j0 : blockDim.x;
+    const uint32_t i0 = first + j0;
+    // the block's values (contiguous over its items) into the slot streams,
+    // and its auth paths behind them
+    const int m = L < 0 ? P.k : LEN;
+    const uint32_t vw = (uint32_t)m * N / 8;
+    // (kCopyBatch loads in flight per thread before their stores: one
+    // memory latency per batch, not per word; the item and word of a load
+    // advance incrementally)
+    const uint32_t i = i0 + threadIdx.x;
+    const bool live = threadIdx.x < nb;
+    SignWork wk;
+    wk.flags = 1;
+    if (live) wk = A.work[i];
+    constexpr int kCopyBatch = 16;
+    const uint2 *src = reinterpret_cast<const uint2 *>((L < 0 ? A.fors_roots : A.wpk) + (uint64_t)i0 * m * N);
+    {
+        uint32_t t = threadIdx.x / vw, q = threadIdx.x - t * vw;
+        for (uint32_t w0 = threadIdx.x; w0 < nb * vw; w0 += kCopyBatch * blockDim.x) {
+            uint2 x[kCopyBatch];
+#pragma unroll
+            for (int k = 0; k < kCopyBatch; k++) {
+                const uint32_t w = w0 + k * blockDim.x;
+                if (w < nb * vw) x[k] = src[w];
+            }
+#pragma unroll
+            for (int k = 0; k < kCopyBatch; k++) {
+                if (w0 + k * blockDim.x < nb * vw) PV::put_value_word(smem + t * stride + PV::S_HDR, (int)q, x[k]);
+                for (q += blockDim.x; q >= vw; q -= vw) t++;
+            }
+        }
+    }
+    if (L >= 0) {
+        const uint32_t aw = (uint32_t)P.hp * W;
+        const uint8_t *sa = A.sig + (uint64_t)i0 * A.sig_stride + sig_layer_off(P, L) + P.wots_bytes;
+        uint32_t t = threadIdx.x / aw, q = threadIdx.x - t * aw;
+        for (uint32_t w0 = threadIdx.x; w0 < nb * aw; w0 += kCopyBatch * blockDim.x) {
+            uint32_t x[kCopyBatch];
+            uint32_t tt = t, qq = q;
+#pragma unroll
+            for (int k = 0; k < kCopyBatch; k++) {
+                if (w0 + k * blockDim.x < nb * aw)
+                    x[k] = *reinterpret_cast<const uint32_t *>(sa + (uint64_t)tt * A.sig_stride + 4ull * qq);
+                for (qq += blockDim.x; qq >= aw; qq -= aw) tt++;
+            }
+#pragma unroll
+            for (int k = 0; k < kCopyBatch; k++) {
+                if (w0 + k * blockDim.x < nb * aw) smem[t * stride + PV::S_HDR + PV::kStreamWords + q] = x[k];
+                for (q += blockDim.x; q >= aw; q -= aw) t++;
+            }
+        }
+    }
+    __syncthreads();
+    const bool ok = live && !wk.flags;
+    const uint8_t *pkb = live ? A.pk.row(i) : nullptr;
+    uint32_t root[W];
+    if (ok) {
+        uint32_t *S = smem + threadIdx.x * stride;
+        uint32_t *stream = S + PV::S_HDR;
+        // the slot's key material and frame, written by this thread alone
+        // (the policy's helpers split them over lanes; all lanes' shares here)
+        for (uint32_t l = 0; l < 32; l++) PV::load_key(S, A.work + i, pkb, l);
+        uint64_t tree_L = wk.tree;
+        uint32_t idx_L = wk.idx_leaf;
+        Adrs pa;
+        adrs_zero(pa);
+        if (L >= 0) {
+            layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+            adrs_layer(pa, L);
+        }
+        adrs_tree(pa, tree_L);
+        adrs_keypair(pa, idx_L);
+        adrs_type(pa, L < 0 ? ADDR_FORSPK : ADDR_WOTSPK);
+        for (uint32_t l = 0; l < 32; l++) PV::frame(stream, S, pa, m, l);
+        Adrs wa;   // the layer's WOTS+ ADRS words, from which build_h derives its own
+        adrs_zero(wa);
+        adrs_layer(wa, L < 0 ? 0 : L);
+        adrs_tree(wa, tree_L);
+        adrs_type(wa, ADDR_WOTS);
+        adrs_keypair(wa, idx_L);
+        S[PV::S_AW0] = wa.w[0];
+        S[PV::S_AW1] = wa.w[1];
+        S[PV::S_AW2] = wa.w[2];
+        S[PV::S_IDXL] = idx_L;
+        S[PV::S_M] = (uint32_t)m;
+        S[PV::S_NB] = (uint32_t)PV::stream_blocks(m);
+        S[PV::S_MASK] = S[PV::S_MASK + 1] = S[PV::S_MASK + 2] = ~0u;   // every value present
+        typename PV::LaneRegs lr{};
+        PV::claim_t(lr, S, P.hp);
+        const int nbk = PV::stream_blocks(m);
+        for (int j = 0; j < nbk;) {
+            typename PV::Unit u;
+            if constexpr (PV::kTMask) {
+                if (PV::t_action(S, j) == 1) {
+                    PV::build_mask(u, S, P.hp);
+                    PV::run(u);
+                    PV::after_mask(u, S, P.hp);
+                    continue;
+                }
+            }
+            PV::build_t(u, lr, S, j, P.hp);
+            PV::run(u);
+            PV::after_t(u, lr, S, P.hp);
+            if (++j == nbk) PV::value_out(u, root);
+        }
+        if (L >= 0) {
+            // compute_root (utils.cu:94-135) over the staged auth path
+            uint32_t idx = idx_L;
+            for (int h = 0; h < P.hp; h++) {
+                for (int sub = 0; sub < PV::kHUnits; sub++) {
+                    typename PV::Unit u;
+                    PV::build_h(u, lr, S, h, sub, idx, root, P.hp);
+                    PV::run(u);
+                    if (sub < PV::kHUnits - 1) PV::after_h_unit(u, lr, sub);
+                    else PV::value_out(u, root);
+                }
+                idx >>= 1;
+            }
+        }
+    }
+    if (L == P.d - 1) {   // uniform over the launch: no barrier follows
+        if (live) {
+            bool eq = ok;
+            if (ok) {
+                uint32_t pr[W];
+                HF::load(pr, pkb + N);
+#pragma unroll
+                for (int x = 0; x < W; x++) eq &= pr[x] == root[x];
+            }
+            A.verdict[i] = eq ? 0 : -1;
+        }
+        return;
+    }
+    // bucket layer L+1's chains: block-local ranks, one global reservation
+    // per bucket and block, then the entries
+    uint32_t *lr = reinterpret_cast<uint32_t *>(reinterpret_cast<uint8_t *>(smem) + SM::lr_off(P, blockDim.x)) +
+                   threadIdx.x * LEN;
+    if (ok) {
+        const uint32_t csum = vsort_checksum<HF>(root);
+#pragma unroll
+        for (int c = 0; c < LEN; c++) {
+            const uint32_t l = vsort_steps<HF>(root, csum, c);
+            lr[c] = l << 16 | atomicAdd(&hcount[l], 1u);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 16 && hcount[threadIdx.x])
+        hbase[threadIdx.x] = atomicAdd(&V.cnt[((uint64_t)grp * P.d + L + 1) * 16 + threadIdx.x], hcount[threadIdx.x]);
+    __syncthreads();
+    if (ok) {
+        uint32_t *base = V.tasks + (uint64_t)first * LEN;
+        for (int c = 0; c < LEN; c++) {
+            const uint32_t e = lr[c], l = e >> 16;
+            base[(uint64_t)l * V.stride + hbase[l] + (e & 0xffffu)] = i << 7 | (uint32_t)c;
+        }
+    }
+}
+
+// One lane per chain of layer L, in sorted order (most steps first; the
+// zero-step chains, plain copies, last): sorted position p of the group ->
+// bucket and entry.
+template <class HF>
+__global__ void __launch_bounds__(128) k_vsort_chains(SetParams P, VerifyArgs A, VerifyLists V, int L,
+                                                      uint32_t first, int grp) {
+    constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
+    __shared__ uint32_t cnt[16];
+    if (threadIdx.x < 16) cnt[threadIdx.x] = V.cnt[((uint64_t)grp * P.d + L) * 16 + threadIdx.x];
+    __syncthreads();
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    int l = 15;
+    for (; l >= 0; l--) {
+        if (p < cnt[l]) break;
+        p -= cnt[l];
+    }
+    if (l < 0) return;
+    const uint32_t e = V.tasks[(uint64_t)first * LEN + (uint64_t)l * V.stride + p];
+    const uint32_t item = e >> 7;
+    const int c = (int)(e & 127u);
+    const SignWork wk = A.work[item];
+    const uint8_t *pkb = A.pk.row(item);
+    KeyRegs<N> key;
+    key_from_work<HF>(key, pkb, pkb, wk);
+    uint64_t tree_L;
+    uint32_t idx_L;
+    layer_index(P, wk.tree, wk.idx_leaf, L, tree_L, idx_L);
+    Adrs wa;
+    adrs_zero(wa);
+    adrs_layer(wa, L);
+    adrs_tree(wa, tree_L);
+    adrs_type(wa, ADDR_WOTS);
+    adrs_keypair(wa, idx_L);
+    adrs_chain(wa, c);
+    typename HF::FCtx fc;
+    HF::f_prepare(fc, wa, key);
+    uint32_t v[W];
+    HF::load(v, A.sig + (uint64_t)item * A.sig_stride + sig_layer_off(P, L) + (uint64_t)c * N);
+    for (uint32_t s = 15u - (uint32_t)l; s < 15u; s++) HF::f_step(v, v, fc, s, key);
+    HF::store(A.wpk + ((uint64_t)item * LEN + c) * N, v);
+}
+
+}  // namespace cuspx

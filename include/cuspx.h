@@ -68,7 +68,8 @@ typedef struct {
     int tree_warps;       /* warps per block, XMSS tree kernel */
     int chains_per_warp;  /* (item, chain) tasks per warp, verify chain kernel */
     int verify_mode;      /* 0 layered verify kernels, 1 one thread per item over all layers,
-                             2 one persistent launch over the whole hypertree (default) */
+                             2 one persistent launch over the whole hypertree (default),
+                             3 layered kernels with each layer's WOTS+ chains sorted by length */
     int fors_lanes_log2;  /* lanes per FORS tree = 2^g, g in 0..5 (0: lane per tree, 5: warp per tree) */
     int tree_mode;        /* 0 warp per XMSS subtree, 1 lane per subtree (heights <= 4 only) */
     int chain_mode_max;   /* batches of at most this many signatures (up to 256) compute XMSS
@@ -83,9 +84,16 @@ typedef struct {
     int verify_claim_min; /* verify_mode 2: WOTS+ chains are handed out to free lanes once at
                              least this many lanes of a warp are free (1..32; T streams always
                              at once) */
+    int verify_groups;    /* sorted verify: the batch is split into this many groups of items
+                             (1..8), each on its own stream, so that one group's serial T_len
+                             and auth-path kernel overlaps another group's chains */
+    int verify_sorted_min;/* verify batches of at least this many items run the sorted layered
+                             verify whatever verify_mode says (0: only with verify_mode 3);
+                             batches up to verify_item_max still run one item per block */
 } cuspx_tuning;
 /* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2,
- * tree_mode, chain_mode_max and verify_item_max, which keep it when < 0 */
+ * tree_mode, chain_mode_max, verify_item_max and verify_sorted_min, which keep
+ * it when < 0 */
 int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
 int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
 /* Mappings by batch size (what the autotuner installs): the mapping of

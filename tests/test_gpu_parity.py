@@ -162,8 +162,11 @@ def test_verify_mappings_agree(engine, setname):
                   {"verify_mode": 2, "verify_slots": 3, "verify_block": 64},
                   {"verify_mode": 2, "verify_slots": 8, "verify_block": 128},
                   {"verify_mode": 2, "verify_slots": 4, "verify_block": 64, "verify_claim_min": 6},
-                  {"verify_mode": 2, "verify_slots": 2, "verify_block": 32, "verify_claim_min": 32}):
-            engine.set_tuning(sid, **dict({"verify_item_max": 0, "verify_claim_min": 1}, **m))
+                  {"verify_mode": 2, "verify_slots": 2, "verify_block": 32, "verify_claim_min": 32},
+                  {"verify_mode": 3, "verify_groups": 1, "verify_block": 32},
+                  {"verify_mode": 3, "verify_groups": 2, "verify_block": 64},
+                  {"verify_mode": 3, "verify_groups": 4, "verify_block": 128}):
+            engine.set_tuning(sid, **dict({"verify_item_max": 0, "verify_claim_min": 1, "verify_sorted_min": 0}, **m))
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
             assert list(got) == want, m
         # one item per block (the small-batch kernel)
@@ -173,14 +176,53 @@ def test_verify_mappings_agree(engine, setname):
         # items into each warp (1300 items on 152 SMs: 3 per warp), and the
         # same batch one item per block (several blocks share each SM)
         rep = 1300
-        for m in ({"verify_mode": 2, "verify_slots": 8, "verify_block": 64, "verify_item_max": 0},
+        for m in ({"verify_mode": 2, "verify_slots": 8, "verify_block": 64, "verify_item_max": 0,
+                   "verify_sorted_min": 0},
                   {"verify_mode": 2, "verify_slots": 4, "verify_block": 64, "verify_item_max": 0,
-                   "verify_claim_min": 8},
+                   "verify_claim_min": 8, "verify_sorted_min": 0},
+                  {"verify_mode": 2, "verify_item_max": 0, "verify_sorted_min": 1000},
+                  {"verify_mode": 3, "verify_groups": 3, "verify_block": 64, "verify_item_max": 0},
                   {"verify_item_max": 2000}):
             engine.set_tuning(sid, **m)
             got = engine.verify_batch(sid, [pks[kidx[i % 12]] for i in range(rep)],
                                       [msgs[i % 12] for i in range(rep)], [sigs[i % 12] for i in range(rep)])
             assert list(got) == [want[i % 12] for i in range(rep)], m
+    finally:
+        engine.set_tuning(sid, **saved)
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "shake256-256f-robust", "sha256-192s-robust"])
+def test_sorted_verify_group_split(engine, setname):
+    """The sorted layered verify (verify_mode 3) splits a batch into item
+    groups on their own streams: batches smaller than the group count, one
+    item, uneven splits and a wrong-length signature inside a group all give
+    the CPU's verdicts, and so do batches the size threshold sends there
+    whatever verify_mode says."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(31)
+    seed = bytes(rng.randrange(256) for _ in range(3 * o.p.n))
+    pk, sk = o.seed_keypair(seed)
+    msgs = [bytes(rng.randrange(256) for _ in range(5 + 11 * i)) for i in range(4)]
+    sigs = [o.sign(m, sk) for m in msgs]
+    bad = bytearray(sigs[1])
+    bad[len(bad) // 2] ^= 0x40
+    cases = [(sigs[0], msgs[0], len(sigs[0])), (bytes(bad), msgs[1], len(bad)),
+             (sigs[2], msgs[2], len(sigs[2]) - 8), (sigs[3], msgs[3], len(sigs[3]))]
+    want = [o.verify(s, m, pk) if ln == len(s) else -1 for s, m, ln in cases]   # wrong length: rejected
+    assert want == [0, -1, -1, 0]
+    saved = engine.get_tuning(sid)
+    try:
+        for count, m in ((1, {"verify_mode": 3, "verify_groups": 4}),
+                         (2, {"verify_mode": 3, "verify_groups": 4}),
+                         (5, {"verify_mode": 3, "verify_groups": 3}),
+                         (37, {"verify_mode": 3, "verify_groups": 4, "verify_block": 128}),
+                         (37, {"verify_mode": 2, "verify_sorted_min": 30, "verify_groups": 2})):
+            engine.set_tuning(sid, **dict({"verify_item_max": 0}, **m))
+            pick = [(i * 7 + 3) % len(cases) for i in range(count)]
+            got = engine.verify_batch(sid, [pk] * count, [cases[j][1] for j in pick], [cases[j][0] for j in pick],
+                                      siglens=[cases[j][2] for j in pick])
+            assert list(got) == [want[j] for j in pick], (count, m)
     finally:
         engine.set_tuning(sid, **saved)
 
@@ -212,8 +254,11 @@ def test_persistent_verify_refills_slots(engine):
     pick = [rng.randrange(len(cases)) for _ in range(count)]
     saved = engine.get_tuning(sid)
     try:
-        for m in ({"verify_mode": 2, "verify_slots": 1, "verify_block": 32, "verify_item_max": 0},
-                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 128, "verify_item_max": 0}):
+        for m in ({"verify_mode": 2, "verify_slots": 1, "verify_block": 32, "verify_item_max": 0,
+                   "verify_sorted_min": 0},
+                  {"verify_mode": 2, "verify_slots": 4, "verify_block": 128, "verify_item_max": 0,
+                   "verify_sorted_min": 0},
+                  {"verify_mode": 3, "verify_groups": 2, "verify_block": 64, "verify_item_max": 0}):
             engine.set_tuning(sid, **m)
             got = engine.verify_batch(sid, [pk] * count, [cases[j][1] for j in pick], [cases[j][0] for j in pick],
                                       siglens=[cases[j][2] for j in pick])

@@ -230,8 +230,8 @@ static size_t item_bytes(int op, const SetParams &P) {
     size_t b = sizeof(SignWork) + P.k * n + 64;
     if (op == CUSPX_OP_SIGN)
         b += P.sig_bytes + n + (size_t)P.d * ((size_t)1 << P.hp) * n + P.d * n + (size_t)P.d * P.len * 16 * n;
-    else
-        b += P.sig_bytes + 8 + (size_t)P.len * n + n;
+    else   // signature, its length, WOTS+ public key, root, sorted-verify bucket entries
+        b += P.sig_bytes + 8 + (size_t)P.len * n + n + 16 * (size_t)P.len * sizeof(uint32_t);
     return b;
 }
 

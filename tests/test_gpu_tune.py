@@ -93,3 +93,35 @@ def test_per_size_entries_cover_their_ranges(monkeypatch, tmp_path):
             assert sigs[0] == o.sign(msgs[0], sk) and sigs[-1] == o.sign(msgs[-1], sk)
     finally:
         eng.close()
+
+
+def test_sorted_verify_knobs(monkeypatch, tmp_path):
+    """verify_groups / verify_sorted_min: per-set defaults, range checks,
+    0 and -1 for the size threshold (off / keep), and the C reader of the
+    tuning file parses both."""
+    import cuspx_gb300 as c
+    monkeypatch.setenv("CUSPX_TUNE_CACHE", str(tmp_path / "none.tsv"))
+    eng = c.Engine(0)
+    try:
+        s128 = c.set_id("sha256-128f-simple")
+        s256 = c.set_id("shake256-256f-simple")
+        assert eng.get_tuning(s128)["verify_sorted_min"] == 1024
+        assert eng.get_tuning(s256)["verify_sorted_min"] == 2048
+        assert eng.get_tuning(s128)["verify_groups"] == 4
+        for bad in ({"verify_groups": 9}, {"verify_mode": 4}):
+            with pytest.raises(c.CuspxError):
+                eng.set_tuning(s128, **bad)
+        eng.set_tuning(s128, verify_sorted_min=0, verify_groups=8)
+        assert eng.get_tuning(s128)["verify_sorted_min"] == 0 and eng.get_tuning(s128)["verify_groups"] == 8
+        eng.set_tuning(s128, verify_groups=0, verify_sorted_min=-1)   # both keep
+        assert eng.get_tuning(s128)["verify_sorted_min"] == 0 and eng.get_tuning(s128)["verify_groups"] == 8
+        eng.set_tuning(s128, verify_sorted_min=1024, verify_groups=4)
+        path = tmp_path / "tune.tsv"
+        path.write_text("%s\tsha256-128f-simple\tverify\t1025\t4096\t2.0\tverify_groups=6,verify_sorted_min=512\n"
+                        % c.device_name())
+        assert eng.load_tuning(str(path)) == 1
+        got = eng.get_tuning_for(s128, c.OP_VERIFY, 4096)
+        assert got["verify_groups"] == 6 and got["verify_sorted_min"] == 512
+        assert eng.get_tuning_for(s128, c.OP_VERIFY, 1024)["verify_groups"] == 4
+    finally:
+        eng.close()

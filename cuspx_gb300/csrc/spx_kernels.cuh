@@ -18,10 +18,13 @@
 //   k_sign_finish   block / signature    FORS pk (T_k), WOTS signatures gathered
 //                                        from the recorded chains
 //
-// Verify: k_verify_msg (+ k_verify_msg_pair) -> k_verify_fors -> the
-// hypertree, either one persistent launch (k_verify_hyper, spx_verify.cuh;
-// the default) or per-layer k_verify_chains + k_verify_root, or k_verify_ht
-// (one thread per item over all layers).
+// Verify: k_verify_msg (+ k_verify_msg_pair / _wide) -> k_verify_fors -> the
+// hypertree: one block per item for small batches (k_verify_item,
+// spx_verify.cuh), one persistent launch for mid-size ones (k_verify_hyper),
+// per-layer kernels over length-sorted chains for large ones
+// (k_vsort_chains + k_vsort_layer, spx_vsort.cuh); or per-layer
+// k_verify_chains + k_verify_root, or k_verify_ht (one thread per item over
+// all layers).
 // Key generation reuses k_leaves / k_trees on the top layer.
 //
 // Reference structure followed (CPU form): crypto_sign_signature sign.cu:1924-1994,

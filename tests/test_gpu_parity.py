@@ -377,6 +377,52 @@ def test_mixed_sets_one_launch_vs_oracle(engine):
         ms.close()
 
 
+def test_group_run_verify_batches(engine):
+    """Verify batches of two sets in one graph launch (cuspx_group_run): one
+    through the sorted layered verify (its item groups fork onto the batch's
+    side streams inside the capture), one through the persistent kernel;
+    verdicts equal the oracle's, on the captured launch and its replay."""
+    import numpy as np
+    import cuspx_gb300 as c
+    rng = random.Random(404)
+    plan = [("sha256-128f-simple", {"verify_item_max": 0, "verify_mode": 3, "verify_groups": 3}),
+            ("shake256-128f-simple", {"verify_item_max": 0, "verify_mode": 2, "verify_sorted_min": 0})]
+    batches, want, saved = [], [], {}
+    try:
+        for name, tune in plan:
+            o = _oracle(name)
+            sid = engine.set_id(name)
+            saved[sid] = engine.get_tuning(sid)
+            engine.set_tuning(sid, **tune)
+            pk, sk = o.seed_keypair(bytes(rng.randrange(256) for _ in range(3 * o.p.n)))
+            msgs = [bytes(rng.randrange(256) for _ in range(rng.randrange(1, 200))) for _ in range(4)]
+            sigs = [o.sign(m, sk) for m in msgs]
+            bad = bytearray(sigs[2])
+            bad[rng.randrange(len(bad))] ^= 0x08
+            sigs[2] = bytes(bad)
+            n = 40
+            pick = [i % 4 for i in range(n)]
+            w = [o.verify(sigs[j], msgs[j], pk) for j in range(4)]
+            assert w.count(-1) == 1
+            want.append([w[j] for j in pick])
+            slab, offs, lens = c.pack_messages([msgs[j] for j in pick])
+            b = engine.batch(c.OP_VERIFY, sid, n, len(slab), 1)
+            b.upload(n, pk, 1, np.zeros(n, dtype=np.uint32), slab, len(slab), offs, lens,
+                     np.frombuffer(b"".join(sigs[j] for j in pick), dtype=np.uint8))
+            batches.append(b)
+        for _ in range(2):   # captured, then replayed
+            assert c.group_run(engine, batches) > 0
+            for b, w in zip(batches, want):
+                v = np.zeros(len(w), dtype=np.int32)
+                b.download(None, None, v)
+                assert list(v) == w
+    finally:
+        for b in batches:
+            b.close()
+        for sid, t in saved.items():
+            engine.set_tuning(sid, **t)
+
+
 @pytest.mark.parametrize("setname", ["sha256-128f-simple", "sha256-192f-simple", "sha256-256f-simple"])
 def test_long_messages_two_warp_hashing(engine, setname):
     """Batches holding messages of 2 KiB and more hash those over two warps

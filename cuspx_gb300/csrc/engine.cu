@@ -294,13 +294,16 @@ int cuspx_create(int device, cuspx_ctx **out) {
         // 1.44 / 1.22 ms (SHAKE-256f and robust SHA-256-192f cross over
         // between 64 and 256 as well)
         t.verify_item_max = 128;
-        // the sorted layered verify from 2048 items, from 1024 for the
-        // SHA-256 f sets and robust SHA-256 at n = 32 (4096 SHA-256-128f
-        // 2.31 ms against 3.65 ms persistent, 1024 items 1.39 / 1.64 ms,
-        // 512 items 1.38 / 1.42 ms; SHAKE-256f 1024 items 4.33 / 4.05 ms,
-        // 2048 items 6.76 / 8.09 ms)
-        t.verify_sorted_min =
-            (sd.hash == 0 && ((!sd.robust && sd.h / sd.d <= 4) || (sd.robust && sd.n == 32))) ? 1024 : 2048;
+        // the sorted layered verify from 2048 items; from 1024 for the
+        // SHA-256 f sets and robust SHA-256, from 512 for robust SHA-256 at
+        // n = 32 and 192f (4096 SHA-256-128f 2.31 ms against 3.65 ms
+        // persistent, 1024 items 1.39 / 1.64 ms, 512 items 1.38 / 1.42 ms;
+        // SHAKE-256f 1024 items 4.33 / 4.05 ms, 2048 items 6.76 / 8.09 ms;
+        // SHA-256-256f-robust 512 items 4.70 / 9.70 ms, SHA-256-128f-robust
+        // 512 items 2.92 / 2.76 ms, 1024 items 2.99 / 3.36 ms)
+        const bool f_set = sd.h / sd.d <= 4;
+        if (sd.hash == 0 && sd.robust) t.verify_sorted_min = (sd.n == 32 || (sd.n == 24 && f_set)) ? 512 : 1024;
+        else t.verify_sorted_min = (sd.hash == 0 && f_set) ? 1024 : 2048;
     }
     if (cudaSetDevice(device) != cudaSuccess) {
         delete c;

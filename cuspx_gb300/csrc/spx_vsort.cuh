@@ -28,7 +28,10 @@
 // another group's chain kernel keeps the ALU pipes full.
 //
 // A chain of zero steps is its signature value: it sorts last, and its lane
-// in the chain kernel copies the value to the WOTS+ public key buffer.
+// in the chain kernel copies the value to the WOTS+ public key buffer.  For
+// robust SHA-256 the chain kernel also xors in the value's share of the
+// T_len mask (MGF1 blocks are independent), which leaves the layer kernel
+// the plain T_len absorb.
 #pragma once
 #include "spx_verify.cuh"
 
@@ -193,6 +196,11 @@ __global__ void k_vsort_layer(SetParams P, VerifyArgs A, VerifyLists V, int L, u
         S[PV::S_MASK] = S[PV::S_MASK + 1] = S[PV::S_MASK + 2] = ~0u;   // every value present
         typename PV::LaneRegs lr{};
         PV::claim_t(lr, S, P.hp);
+        if constexpr (HF::kRobust && !HF::kShake) {
+            // T_len's values arrive masked from the chain kernel: every mask
+            // unit reads as done and the slot's mask stream stays zero
+            if (L >= 0) S[PV::S_MB] = (uint32_t)(PV::kMB * ((m * N + 31) / 32));
+        }
         const int nbk = PV::stream_blocks(m);
         for (int j = 0; j < nbk;) {
             typename PV::Unit u;
@@ -301,6 +309,30 @@ __global__ void __launch_bounds__(128) k_vsort_chains(SetParams P, VerifyArgs A,
     uint32_t v[W];
     HF::load(v, A.sig + (uint64_t)item * A.sig_stride + sig_layer_off(P, L) + (uint64_t)c * N);
     for (uint32_t s = 15u - (uint32_t)l; s < 15u; s++) HF::f_step(v, v, fc, s, key);
+    if constexpr (HF::kRobust && !HF::kShake) {
+        // Robust SHA-256: T_len absorbs its values xored with MGF1 blocks
+        // SHA256(PUB_SEED || ADRS_T || ctr), independent of one another, so
+        // each chain xors in the mask words over its own value here and the
+        // layer kernel absorbs T_len without computing the mask stream.
+        Adrs ta;
+        adrs_zero(ta);
+        adrs_layer(ta, L);
+        adrs_tree(ta, tree_L);
+        adrs_keypair(ta, idx_L);
+        adrs_type(ta, ADDR_WOTSPK);
+        const uint32_t q0 = (uint32_t)c * W, b0 = q0 >> 3, b1 = (q0 + W - 1) >> 3;
+        uint32_t m0[8], m1[8];
+        HF::mask_block(m0, key.pub, ta, b0);
+        if (b1 != b0) HF::mask_block(m1, key.pub, ta, b1);
+#pragma unroll
+        for (int i = 0; i < W; i++) {
+            const uint32_t q = q0 + i, k = q & 7;
+            uint32_t mw = 0;
+#pragma unroll
+            for (int t = 0; t < 8; t++) mw = (uint32_t)t == k ? ((q >> 3) == b0 ? m0[t] : m1[t]) : mw;
+            v[i] ^= mw;
+        }
+    }
     HF::store(A.wpk + ((uint64_t)item * LEN + c) * N, v);
 }
 

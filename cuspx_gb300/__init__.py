@@ -42,7 +42,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [(f, ctypes.c_int) for f in ("leaf_block", "fors_block", "verify_block", "tree_warps",
                                             "chains_per_warp", "verify_mode", "fors_lanes_log2", "tree_mode",
                                             "chain_mode_max", "verify_slots", "verify_item_max",
-                                            "verify_claim_min", "verify_groups", "verify_sorted_min")]
+                                            "verify_claim_min", "verify_groups", "verify_sorted_min",
+                                            "verify_spec_max")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -200,7 +201,7 @@ class Engine:
 
     def set_tuning(self, sid, **kw):
         """Change fields of a set's launch mapping (others keep their value)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1, 0, 0, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1, 0, 0, -1, -1)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning(self.h, sid, ctypes.byref(t)), "set_tuning")
@@ -213,7 +214,7 @@ class Engine:
     def set_tuning_for(self, sid, op, min_count, max_count, **kw):
         """Mapping of (set, op) for batches of min_count..max_count items
         (fields not given keep the set's base mapping)."""
-        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1, 0, 0, -1)
+        t = Tuning(0, 0, 0, 0, 0, -1, -1, -1, -1, 0, -1, 0, 0, -1, -1)
         for k, v in kw.items():
             setattr(t, k, int(v))
         self._check(self.L.cuspx_set_tuning_for(self.h, sid, op, min_count, max_count, ctypes.byref(t)),

@@ -44,6 +44,7 @@ SIGN_SPACE = {
 VERIFY_SPACE = {
     "verify_item_max": [0, None],   # None: this bucket's size (one item per block)
     "verify_sorted_min": [0, 1],    # 1: every batch of this bucket verifies as verify_mode 3
+    "verify_spec_max": [0, None],   # None: this bucket's size (speculative chains, up to 64 items)
     "verify_mode": [0, 1, 2, 3],
     "verify_slots": [2, 3, 4, 6, 8],
     "chains_per_warp": [32, 64, 128, 256, 512],
@@ -52,6 +53,7 @@ VERIFY_SPACE = {
     "verify_groups": [2, 4, 6, 8],
 }
 OP_NAMES = {OP_SIGN: "sign", OP_VERIFY: "verify"}
+SPEC_MAX_ITEMS = 64   # largest verify_spec_max the library accepts
 
 
 def cache_path():
@@ -151,6 +153,8 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2,
         batch = vb
     space = {k: [b if v is None else v for v in vals]
              for k, vals in (SIGN_SPACE if op == OP_SIGN else VERIFY_SPACE).items()}
+    if "verify_spec_max" in space and b > SPEC_MAX_ITEMS:   # the speculative path covers up to 64 items
+        space["verify_spec_max"] = [0]
     cur = {k: v for k, v in eng.get_tuning_for(sid, op, count).items() if k in space}
     eng.set_tuning_for(sid, op, *bucket_range(b), **cur)
     best_ms = _time(batch, reps)

@@ -82,6 +82,9 @@ using namespace cuspx;
 // items per batch for which chain-parallel leaf scratch is allocated (the
 // largest chain_mode_max that can take effect)
 static const size_t kChainModeItems = 256;
+// items per verify batch that the speculative chain table covers (the
+// largest verify_spec_max; 64 x 22 x 35 x 16 x 16 B = 12.6 MB at 128f)
+static const int kSpecItems = 64;
 // keys per key-generation batch that the chain-parallel scratch covers
 // (16384 x 2^hp x len x n: 73 MB at 128f)
 static const size_t kKeygenChainItems = 16384;
@@ -301,6 +304,12 @@ int cuspx_create(int device, cuspx_ctx **out) {
         // SHAKE-256f 1024 items 4.33 / 4.05 ms, 2048 items 6.76 / 8.09 ms;
         // SHA-256-256f-robust 512 items 4.70 / 9.70 ms, SHA-256-128f-robust
         // 512 items 2.92 / 2.76 ms, 1024 items 2.99 / 3.36 ms)
+        // speculative chains up to 32 items, 64 for robust SHA-256 (1 item
+        // SHA-256-128f 0.54 ms against 0.88 ms one block per item, 32 items
+        // 0.78 / 0.87 ms, 64 items 0.95 / 0.88 ms; SHA-256-192f-robust 1 item
+        // 1.62 / 3.33 ms, 64 items 2.83 / 3.47 ms; SHAKE-256f 1 item 2.01 /
+        // 3.09 ms, 32 items 3.03 / 3.12 ms)
+        t.verify_spec_max = (sd.hash == 0 && sd.robust) ? 64 : 32;
         const bool f_set = sd.h / sd.d <= 4;
         if (sd.hash == 0 && sd.robust) t.verify_sorted_min = (sd.n == 32 || (sd.n == 24 && f_set)) ? 512 : 1024;
         else t.verify_sorted_min = (sd.hash == 0 && f_set) ? 1024 : 2048;
@@ -406,6 +415,10 @@ static int merge_tuning(cuspx_ctx *ctx, const Tuning &base, const cuspx_tuning *
         t.verify_groups = in->verify_groups;
     }
     if (in->verify_sorted_min >= 0) t.verify_sorted_min = in->verify_sorted_min;
+    if (in->verify_spec_max >= 0) {
+        if (in->verify_spec_max > kSpecItems) return fail(ctx, CUSPX_EINVAL, "verify_spec_max must be in 0..64");
+        t.verify_spec_max = in->verify_spec_max;
+    }
     out = t;
     return CUSPX_OK;
 }
@@ -470,6 +483,7 @@ static void to_abi(const Tuning &t, cuspx_tuning *out) {
     out->verify_claim_min = t.verify_claim_min;
     out->verify_groups = t.verify_groups;
     out->verify_sorted_min = t.verify_sorted_min;
+    out->verify_spec_max = t.verify_spec_max;
 }
 
 int cuspx_get_tuning_for(cuspx_ctx *ctx, int set, int op, size_t count, cuspx_tuning *out) {
@@ -540,7 +554,7 @@ static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
         t.leaf_block = t.fors_block = t.verify_block = t.tree_warps = t.chains_per_warp = t.verify_slots = 0;
         t.verify_mode = t.fors_lanes_log2 = t.tree_mode = t.chain_mode_max = t.verify_item_max = -1;
         t.verify_claim_min = t.verify_groups = 0;
-        t.verify_sorted_min = -1;
+        t.verify_sorted_min = t.verify_spec_max = -1;
         bool ok = true;
         size_t at = 0;
         const std::string &kv = col[6];
@@ -570,6 +584,7 @@ static int load_tuning_file(cuspx_ctx *ctx, const char *path, bool quiet) {
             else if (k == "verify_claim_min") t.verify_claim_min = v;
             else if (k == "verify_groups") t.verify_groups = v;
             else if (k == "verify_sorted_min") t.verify_sorted_min = v;
+            else if (k == "verify_spec_max") t.verify_spec_max = v;
             else ok = false;
         }
         if (ok && cuspx_set_tuning_for(ctx, set, op, (size_t)lo, (size_t)hi, &t) == CUSPX_OK) installed++;
@@ -850,11 +865,32 @@ static void collect_profile(cuspx_batch *b) {
     }
 }
 
+// The speculative chain table of a verify batch, allocated the first time a
+// batch runs at a size the speculative path takes (outside any capture: the
+// first run of a shape is a direct launch, and group_run calls this before
+// it captures).  If the allocation fails the batch verifies without it.
+static void spec_scratch(cuspx_batch *b) {
+    if (b->op != CUSPX_OP_VERIFY || b->vlists.cand) return;
+    const Tuning &tu = effective_tuning(b->ctx, b->set, b->op, b->count);
+    if (tu.verify_spec_max <= 0 || b->count > (size_t)tu.verify_spec_max) return;
+    const SetParams &P = b->P;
+    const size_t items = std::min<size_t>(b->cap, kSpecItems);
+    void *p = nullptr;
+    if (cudaMalloc(&p, items * P.d * P.len * 16 * P.n) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    b->allocs.push_back(p);
+    b->vlists.cand = (uint8_t *)p;
+    b->vlists.cand_items = (uint32_t)items;
+}
+
 int cuspx_batch_run(cuspx_batch *b) {
     if (!b) return CUSPX_EINVAL;
     cuspx_ctx *ctx = b->ctx;
     CK(cudaSetDevice(ctx->device), ctx);
     if (b->count == 0) return CUSPX_OK;
+    spec_scratch(b);
     if (b->profile) {
         collect_profile(b);
         b->pt.n = 0;
@@ -1354,6 +1390,7 @@ int cuspx_group_run(cuspx_ctx *ctx, cuspx_batch *const *batches, int nb, float *
     // the batches' uploads (on their own streams) must be complete before the
     // streams join a capture or the graph reads their buffers
     for (int i = 0; i < nb; i++) CK(cudaStreamSynchronize(batches[i]->s), ctx);
+    for (int i = 0; i < nb; i++) spec_scratch(batches[i]);
     cuspx_ctx::GroupGraph *hit = nullptr;
     for (auto &g : ctx->groups) {
         if ((int)g.batches.size() != nb) continue;

@@ -31,6 +31,7 @@ struct Tuning {
     int verify_claim_min = 1;// persistent verify: free lanes before chains are handed out
     int verify_groups = 4;   // sorted verify: item groups on their own streams (1..8)
     int verify_sorted_min = 0; // batches of at least this many items verify as verify_mode 3 (0: never by size)
+    int verify_spec_max = 0;   // batches of at most this many items verify with speculative chains (0: never)
 };
 
 struct KeygenArgs {
@@ -152,6 +153,7 @@ struct Family {
                 return e;
         if ((e = cudaFuncSetAttribute(k_verify_item<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_vsort_layer<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_vspec_walk<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         // Load every other kernel of the family now: with lazy module loading
         // a kernel's first launch loads it, and in a server that first launch
         // is a request's (one took ~50 ms of host time and held back every
@@ -161,6 +163,7 @@ struct Family {
                               (const void *)k_trees_lane<HF>, (const void *)k_sign_finish<HF>,
                               (const void *)k_verify_msg<HF>, (const void *)k_verify_fors<HF>,
                               (const void *)k_verify_chains<HF>, (const void *)k_vsort_chains<HF>,
+                              (const void *)k_vspec_cand<HF>,
                               (const void *)k_keygen_finish<N>};
         for (const void *f : rest)
             if ((e = cudaFuncGetAttributes(&fa, f))) return e;
@@ -363,6 +366,32 @@ struct Family {
                             P.len2 == 3 && !(tu.verify_item_max > 0 && A.count <= (uint32_t)tu.verify_item_max);
         if (sorted) {   // FORS per item group, beside the other groups' layers
             verify_sorted(P, A, tu, s, pt, *vl, vf);
+            return;
+        }
+        if (tu.verify_spec_max > 0 && A.count <= (uint32_t)tu.verify_spec_max && vl && vl->cand &&
+            A.count <= vl->cand_items && 32u * VsortSmem<HF>::slot_stride(P.hp) * 4u <= kLayerSmem &&
+            P.len1 == 2 * N && P.len2 == 3) {
+            // tiny batches: every chain run from every start step, then the
+            // serial walk over T_len and the auth paths alone (spx_vsort.cuh)
+            // (the chain runs beside the FORS roots, on a side stream)
+            constexpr int LEN = 2 * N + 3;
+            const bool side = !pt && vf && vf->sides > 0;
+            cudaStream_t cs = side ? vf->side[0] : s;
+            if (side) {
+                cudaEventRecord(vf->fork, s);
+                cudaStreamWaitEvent(cs, vf->fork, 0);
+            }
+            k_vspec_cand<HF><<<ceil_div(16ull * A.count * P.d * LEN, 128), 128, 0, cs>>>(P, A, vl->cand);
+            CUSPX_MARK(pt, "k_vspec_cand", s);
+            k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A, 0, A.count);
+            CUSPX_MARK(pt, "k_verify_fors", s);
+            if (side) {
+                cudaEventRecord(vf->join[0], cs);
+                cudaStreamWaitEvent(s, vf->join[0], 0);
+            }
+            k_vspec_walk<HF><<<ceil_div(A.count, 32), 32, 32u * VsortSmem<HF>::slot_stride(P.hp) * 4u, s>>>(
+                P, A, vl->cand);
+            CUSPX_MARK(pt, "k_vspec_walk", s);
             return;
         }
         k_verify_fors<HF><<<ceil_div((uint64_t)A.count * P.k, 128), 128, 0, s>>>(P, A, 0, A.count);

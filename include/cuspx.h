@@ -90,10 +90,14 @@ typedef struct {
     int verify_sorted_min;/* verify batches of at least this many items run the sorted layered
                              verify whatever verify_mode says (0: only with verify_mode 3);
                              batches up to verify_item_max still run one item per block */
+    int verify_spec_max;  /* verify batches of at most this many items (0..64; 0: never) first
+                             run every WOTS+ chain of every layer from each of its 16 possible
+                             start steps in parallel, then walk the layers with T_len and the
+                             auth path alone (takes precedence over verify_item_max) */
 } cuspx_tuning;
 /* fields <= 0 keep the current value, except verify_mode, fors_lanes_log2,
- * tree_mode, chain_mode_max, verify_item_max and verify_sorted_min, which keep
- * it when < 0 */
+ * tree_mode, chain_mode_max, verify_item_max, verify_sorted_min and
+ * verify_spec_max, which keep it when < 0 */
 int cuspx_set_tuning(cuspx_ctx *ctx, int set, const cuspx_tuning *t);
 int cuspx_get_tuning(cuspx_ctx *ctx, int set, cuspx_tuning *t);
 /* Mappings by batch size (what the autotuner installs): the mapping of

@@ -165,12 +165,14 @@ def test_verify_mappings_agree(engine, setname):
                   {"verify_mode": 2, "verify_slots": 2, "verify_block": 32, "verify_claim_min": 32},
                   {"verify_mode": 3, "verify_groups": 1, "verify_block": 32},
                   {"verify_mode": 3, "verify_groups": 2, "verify_block": 64},
-                  {"verify_mode": 3, "verify_groups": 4, "verify_block": 128}):
-            engine.set_tuning(sid, **dict({"verify_item_max": 0, "verify_claim_min": 1, "verify_sorted_min": 0}, **m))
+                  {"verify_mode": 3, "verify_groups": 4, "verify_block": 128},
+                  {"verify_spec_max": 16}):
+            engine.set_tuning(sid, **dict({"verify_item_max": 0, "verify_claim_min": 1, "verify_sorted_min": 0,
+                                            "verify_spec_max": 0}, **m))
             got = engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)
             assert list(got) == want, m
         # one item per block (the small-batch kernel)
-        engine.set_tuning(sid, verify_item_max=64)
+        engine.set_tuning(sid, verify_item_max=64, verify_spec_max=0)
         assert list(engine.verify_batch(sid, [pks[k] for k in kidx], msgs, sigs)) == want
         # a batch large enough that the persistent kernel packs several
         # items into each warp (1300 items on 152 SMs: 3 per warp), and the
@@ -218,11 +220,42 @@ def test_sorted_verify_group_split(engine, setname):
                          (5, {"verify_mode": 3, "verify_groups": 3}),
                          (37, {"verify_mode": 3, "verify_groups": 4, "verify_block": 128}),
                          (37, {"verify_mode": 2, "verify_sorted_min": 30, "verify_groups": 2})):
-            engine.set_tuning(sid, **dict({"verify_item_max": 0}, **m))
+            engine.set_tuning(sid, **dict({"verify_item_max": 0, "verify_spec_max": 0}, **m))
             pick = [(i * 7 + 3) % len(cases) for i in range(count)]
             got = engine.verify_batch(sid, [pk] * count, [cases[j][1] for j in pick], [cases[j][0] for j in pick],
                                       siglens=[cases[j][2] for j in pick])
             assert list(got) == [want[j] for j in pick], (count, m)
+    finally:
+        engine.set_tuning(sid, **saved)
+
+
+@pytest.mark.parametrize("setname", ["sha256-128f-simple", "sha256-192f-robust", "shake256-256f-robust",
+                                     "shake256-128s-simple"])
+def test_speculative_verify(engine, setname):
+    """Tiny batches verified from speculative chain runs (every chain of every
+    layer from each of its 16 start steps, then the serial T_len / auth-path
+    walk): one item, a few, the 64-item maximum, corrupted and wrong-length
+    signatures, all equal to the CPU's verdicts."""
+    o = _oracle(setname)
+    sid = engine.set_id(setname)
+    rng = random.Random(61)
+    pk, sk = o.seed_keypair(bytes(rng.randrange(256) for _ in range(3 * o.p.n)))
+    msgs = [bytes(rng.randrange(256) for _ in range(3 + 29 * i)) for i in range(4)]
+    sigs = [o.sign(m, sk) for m in msgs]
+    bad = bytearray(sigs[1])
+    bad[rng.randrange(len(bad))] ^= 0x02
+    cases = [(sigs[0], msgs[0], len(sigs[0])), (bytes(bad), msgs[1], len(bad)),
+             (sigs[2], msgs[2], len(sigs[2]) + 1), (sigs[3], msgs[3], len(sigs[3]))]
+    want = [o.verify(sg, m, pk) if ln == len(sg) else -1 for sg, m, ln in cases]   # wrong length: rejected
+    assert want == [0, -1, -1, 0]
+    saved = engine.get_tuning(sid)
+    try:
+        engine.set_tuning(sid, verify_spec_max=64, verify_item_max=0)
+        for count in (1, 3, 64):
+            pick = [(i * 5 + 3) % len(cases) for i in range(count)] if count > 1 else [0]
+            got = engine.verify_batch(sid, [pk] * count, [cases[j][1] for j in pick], [cases[j][0] for j in pick],
+                                      siglens=[cases[j][2] for j in pick])
+            assert list(got) == [want[j] for j in pick], count
     finally:
         engine.set_tuning(sid, **saved)
 

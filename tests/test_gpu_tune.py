@@ -96,7 +96,7 @@ def test_per_size_entries_cover_their_ranges(monkeypatch, tmp_path):
 
 
 def test_sorted_verify_knobs(monkeypatch, tmp_path):
-    """verify_groups / verify_sorted_min: per-set defaults, range checks,
+    """verify_groups / verify_sorted_min / verify_spec_max: per-set defaults, range checks,
     0 and -1 for the size threshold (off / keep), and the C reader of the
     tuning file parses both."""
     import cuspx_gb300 as c
@@ -108,7 +108,9 @@ def test_sorted_verify_knobs(monkeypatch, tmp_path):
         assert eng.get_tuning(s128)["verify_sorted_min"] == 1024
         assert eng.get_tuning(s256)["verify_sorted_min"] == 2048
         assert eng.get_tuning(s128)["verify_groups"] == 4
-        for bad in ({"verify_groups": 9}, {"verify_mode": 4}):
+        assert eng.get_tuning(s128)["verify_spec_max"] == 32
+        assert eng.get_tuning(c.set_id("sha256-192f-robust"))["verify_spec_max"] == 64
+        for bad in ({"verify_groups": 9}, {"verify_mode": 4}, {"verify_spec_max": 65}):
             with pytest.raises(c.CuspxError):
                 eng.set_tuning(s128, **bad)
         eng.set_tuning(s128, verify_sorted_min=0, verify_groups=8)

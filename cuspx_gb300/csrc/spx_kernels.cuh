@@ -19,8 +19,10 @@
 //                                        from the recorded chains
 //
 // Verify: k_verify_msg (+ k_verify_msg_pair / _wide) -> k_verify_fors -> the
-// hypertree: one block per item for small batches (k_verify_item,
-// spx_verify.cuh), one persistent launch for mid-size ones (k_verify_hyper),
+// hypertree: for tiny batches every chain run from all 16 start steps, then a
+// serial walk (k_vspec_cand + k_vspec_walk, spx_vsort.cuh), one block per
+// item for small batches (k_verify_item, spx_verify.cuh), one persistent
+// launch for mid-size ones (k_verify_hyper),
 // per-layer kernels over length-sorted chains for large ones
 // (k_vsort_chains + k_vsort_layer, spx_vsort.cuh); or per-layer
 // k_verify_chains + k_verify_root, or k_verify_ht (one thread per item over

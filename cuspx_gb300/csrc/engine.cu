@@ -196,6 +196,7 @@ struct cuspx_batch {
     bool ran = false;
     bool profile = false;
     bool direct = false;   // never capture graphs (serving: see batch_direct_launch)
+    bool no_spec = false;  // never verify through speculative chain runs (serving)
     bool prof_pending = false;
     PhaseTimer pt;
     std::vector<ProfEntry> prof;
@@ -870,7 +871,7 @@ static void collect_profile(cuspx_batch *b) {
 // first run of a shape is a direct launch, and group_run calls this before
 // it captures).  If the allocation fails the batch verifies without it.
 static void spec_scratch(cuspx_batch *b) {
-    if (b->op != CUSPX_OP_VERIFY || b->vlists.cand) return;
+    if (b->op != CUSPX_OP_VERIFY || b->vlists.cand || b->no_spec) return;
     const Tuning &tu = effective_tuning(b->ctx, b->set, b->op, b->count);
     if (tu.verify_spec_max <= 0 || b->count > (size_t)tu.verify_spec_max) return;
     const SetParams &P = b->P;
@@ -1023,6 +1024,24 @@ void batch_direct_launch(cuspx_batch *b, bool on) {
         cudaEventDestroy(b->fork.fork);
         cudaEventDestroy(b->fork.join);
         b->fork = StreamFork{};
+    }
+    // Likewise a verify batch's side streams (the sorted verify's item
+    // groups then share the launch stream).  And no speculative chain runs:
+    // they cost ~15 times a verify's chain work, a latency trade for an idle
+    // GPU, and under a served load that work queues every other request
+    // (a three-set stream at 20k req/s: sign p99 6.6 -> 138 ms).
+    if (on) {
+        b->no_spec = true;
+        for (int g = 0; g + 1 < VerifyFork::kMaxGroups; g++) {
+            if (b->vfork.side[g]) {
+                cudaStreamSynchronize(b->vfork.side[g]);
+                cudaStreamDestroy(b->vfork.side[g]);
+            }
+            if (b->vfork.join[g]) cudaEventDestroy(b->vfork.join[g]);
+            if (b->vfork.chain[g]) cudaEventDestroy(b->vfork.chain[g]);
+        }
+        if (b->vfork.fork) cudaEventDestroy(b->vfork.fork);
+        b->vfork = VerifyFork{};
     }
 }
 

@@ -1,4 +1,7 @@
-// spx_vsort.cuh -- layered verify with the WOTS+ chains sorted by length.
+// spx_vsort.cuh -- verify kernels that reorganise the WOTS+ chain work:
+// layered kernels over each layer's chains sorted by length (large batches,
+// this header's first part) and speculative chain runs followed by a serial
+// walk (tiny batches, at the end).
 //
 // crypto_sign_verify (sign.cu:3048-3121) is serial over the d layers of an
 // item, and per layer a WOTS+ chain c runs 15 - d_c steps of F

@@ -191,11 +191,14 @@ __global__ void k_sign_msg(SetParams P, SignArgs A, uint64_t long_msg) {
     const uint8_t *m = A.msg.base + A.msg.off[i];
     const uint64_t mlen = A.msg.len[i];
     if (long_msg && mlen >= long_msg) return;   // k_sign_msg_pair / k_sign_msg_wide hash it
-    HF::prf_msg(R, skprf, opt, m, mlen);
-    uint8_t *sig = A.sig + (uint64_t)i * P.sig_bytes;
-    HF::store(sig, R);
     uint8_t dg[64];
-    HF::h_msg(dg, P.dgst_bytes, R, pk, m, mlen);
+    if constexpr (!HF::kShake) {
+        HF::msg_digests(R, true, skprf, opt, pk, m, mlen, dg, P.dgst_bytes);
+    } else {
+        HF::prf_msg(R, skprf, opt, m, mlen);
+        HF::h_msg(dg, P.dgst_bytes, R, pk, m, mlen);
+    }
+    HF::store(A.sig + (uint64_t)i * P.sig_bytes, R);
     A.work[i] = work_from_digest<HF>(P, dg, sk + 2 * N);
 }
 
@@ -836,7 +839,9 @@ __global__ void k_verify_msg(SetParams P, VerifyArgs A, uint64_t long_msg) {
     HF::load(pk, pkb);
     HF::load(pk + W, pkb + N);
     uint8_t dg[64];
-    HF::h_msg(dg, P.dgst_bytes, R, pk, A.msg.base + A.msg.off[i], A.msg.len[i]);
+    if constexpr (!HF::kShake) HF::msg_digests(R, false, R, R, pk, A.msg.base + A.msg.off[i], A.msg.len[i], dg,
+                                               P.dgst_bytes);
+    else HF::h_msg(dg, P.dgst_bytes, R, pk, A.msg.base + A.msg.off[i], A.msg.len[i]);
     A.work[i] = work_from_digest<HF>(P, dg, pkb);
 }
 

@@ -503,6 +503,92 @@ struct Sha2 {
         hmac_finish(R, st, skprf);
     }
 
+    // PRF_msg (when with_prf; otherwise R is given) and H_msg of one message
+    // through a single compression call site: the HMAC ipad block, optrand
+    // || m, the opad block, the inner digest, R || PK || m and the MGF1
+    // counter blocks run as one sequence of blocks.  With a call site per
+    // step (prf_msg + h_msg) a thread hashing alone on its SM runs a fresh
+    // ~20 KB copy of the unrolled rounds at every step and waits on
+    // instruction fetch; here one copy stays in the instruction cache.
+    // dg: dgst_bytes digest bytes (a byte array in registers/local).
+    SPX_DEV static void msg_digests(uint32_t R[W], bool with_prf, const uint32_t skprf[W],
+                                    const uint32_t optrand[W], const uint32_t pk[2 * W], const uint8_t *m,
+                                    uint64_t mlen, uint8_t *dg, int dgst_bytes) {
+        const uint64_t nb1 = (4ull * W + mlen + 9 + 63) / 64;   // optrand || m, after the ipad block
+        const uint64_t bits1 = (64 + 4ull * W + mlen) * 8;
+        const uint64_t nb2 = (12ull * W + mlen + 9 + 63) / 64;  // R || PK || m
+        const uint64_t bits2 = (12ull * W + mlen) * 8;
+        const uint64_t nm = (uint64_t)(dgst_bytes + 31) / 32;   // MGF1 blocks
+        uint32_t st[8], keep[8], pre[3 * W], nxt[16];
+        bool have = false;
+        int phase = with_prf ? 0 : 4;   // 0 ipad, 1 optrand || m, 2 opad, 3 inner digest, 4 R || PK || m, 5 MGF1
+        uint64_t b = 0;
+#pragma unroll
+        for (int i = 0; i < W; i++) {
+            pre[i] = with_prf ? 0u : R[i];   // with_prf: R comes from phase 3
+            pre[W + i] = pk[i];
+            pre[2 * W + i] = pk[W + i];
+        }
+        sha256_iv(st);
+        for (;;) {
+            uint32_t w[16];
+            if (phase == 0 || phase == 2) {
+                const uint32_t pad = phase == 0 ? 0x36363636u : 0x5c5c5c5cu;
+#pragma unroll
+                for (int i = 0; i < 16; i++) w[i] = (i < W ? skprf[i] : 0u) ^ pad;
+            } else if (phase == 1) {
+                next_block<W>(w, b, nb1, bits1, optrand, m, mlen, nxt, have);
+            } else if (phase == 4) {
+                next_block<3 * W>(w, b, nb2, bits2, pre, m, mlen, nxt, have);
+            } else {
+                // 3: inner digest || padding (64 + 32 bytes); 5: seed || BE32(b) || padding (36 bytes)
+#pragma unroll
+                for (int i = 0; i < 8; i++) w[i] = keep[i];
+                w[8] = phase == 3 ? 0x80000000u : (uint32_t)b;
+                w[9] = phase == 3 ? 0u : 0x80000000u;
+#pragma unroll
+                for (int i = 10; i < 15; i++) w[i] = 0;
+                w[15] = phase == 3 ? (64 + 32) * 8 : 36 * 8;
+            }
+            sha256_compress(st, w);
+            if (phase == 0) {
+                phase = 1;
+                b = 0;
+                have = false;
+            } else if (phase == 1) {
+                if (++b == nb1) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) keep[i] = st[i];
+                    sha256_iv(st);
+                    phase = 2;
+                }
+            } else if (phase == 2) {
+                phase = 3;
+            } else if (phase == 3) {
+#pragma unroll
+                for (int i = 0; i < W; i++) R[i] = pre[i] = st[i];
+                sha256_iv(st);
+                phase = 4;
+                b = 0;
+                have = false;
+            } else if (phase == 4) {
+                if (++b == nb2) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) keep[i] = st[i];
+                    sha256_iv(st);
+                    phase = 5;
+                    b = 0;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 32; i++)
+                    if (32 * (int)b + i < dgst_bytes) dg[32 * b + i] = (uint8_t)(st[i >> 2] >> (24 - 8 * (i & 3)));
+                sha256_iv(st);
+                if (++b == nm) break;
+            }
+        }
+    }
+
     // H_msg = MGF1-SHA256(SHA256(R || PK || m), dgst) (hash_sha256.cu:200-262);
     // writes dgst_bytes bytes to dg (a byte array in registers/local).
     SPX_DEV static void mgf1_digest(uint8_t *dg, int dgst_bytes, const uint32_t seed[8]) {

@@ -539,8 +539,21 @@ __global__ void k_leaf_chains(SetParams P, LeafArgs A) {
     HF::store(A.ends + gid * N, v);
 }
 
+// T_l of m n-byte values in global memory under ADRS pa into out, by one
+// thread over a slot of `VsortSmem<HF>::slot_stride(0)` shared words
+// (spx_vsort.cuh): the values staged with their loads in flight together,
+// then the hash unit by unit through one call site.
 template <class HF>
-__global__ void k_leaf_tlen(SetParams P, LeafArgs A) {
+SPX_DEV void slot_tl(uint32_t *S, const KeyRegs<4 * HF::W> &key, const uint8_t *pub, const Adrs &pa,
+                     const uint8_t *vals, int m, uint32_t out[HF::W]);
+
+// thread per WOTS+ leaf: T_len over its chain ends, through a slot of
+// slot_words shared words per thread (slot_tl; small sign batches, where the
+// thread's serial latency is what counts), or with slot_words 0 through the
+// T stream of HF::kSmemWords shared words per thread (key generation's
+// large batches, where the smaller footprint keeps more warps resident).
+template <class HF>
+__global__ void k_leaf_tlen(SetParams P, LeafArgs A, uint32_t slot_words) {
     constexpr int W = HF::W, N = 4 * W, LEN = 2 * N + 3;
     extern __shared__ uint32_t smem[];
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -567,16 +580,20 @@ __global__ void k_leaf_tlen(SetParams P, LeafArgs A) {
     adrs_tree(pa, tree_L);
     adrs_type(pa, ADDR_WOTSPK);
     adrs_keypair(pa, j);
-    typename HF::TStream ts;
-    HF::t_init(ts, smem + threadIdx.x * HF::kSmemWords, key, pa);
-    const uint8_t *e = A.ends + gid * LEN * N;
-    for (int c = 0; c < LEN; c++) {
-        uint32_t v[W];
-        HF::load(v, e + (uint64_t)c * N);
-        HF::t_absorb(ts, v, key);
-    }
     uint32_t leaf[W];
-    HF::t_final(leaf, ts);
+    const uint8_t *e = A.ends + gid * LEN * N;
+    if (slot_words) {
+        slot_tl<HF>(smem + threadIdx.x * slot_words, key, sk + 2 * N, pa, e, LEN, leaf);
+    } else {
+        typename HF::TStream ts;
+        HF::t_init(ts, smem + threadIdx.x * HF::kSmemWords, key, pa);
+        for (int c = 0; c < LEN; c++) {
+            uint32_t v[W];
+            HF::load(v, e + (uint64_t)c * N);
+            HF::t_absorb(ts, v, key);
+        }
+        HF::t_final(leaf, ts);
+    }
     HF::store(A.leaves + gid * N, leaf);
 }
 
@@ -747,7 +764,7 @@ __global__ void k_sign_finish(SetParams P, SignArgs A) {
     const uint32_t item = blockIdx.x;
     if (item >= A.count) return;
     uint32_t *forspk = smem;                   // W words
-    uint32_t *tbuf = smem + 8;                 // TStream scratch
+    uint32_t *slot = smem + 8;                 // slot_tl scratch
     const SignWork wk = A.work[item];
     const uint8_t *sk = A.sk.row(item);
     if (threadIdx.x == 0) {
@@ -758,15 +775,8 @@ __global__ void k_sign_finish(SetParams P, SignArgs A) {
         adrs_tree(pa, wk.tree);
         adrs_keypair(pa, wk.idx_leaf);
         adrs_type(pa, ADDR_FORSPK);
-        typename HF::TStream ts;
-        HF::t_init(ts, tbuf, key, pa);
-        for (int t = 0; t < P.k; t++) {
-            uint32_t v[W];
-            HF::load(v, A.fors_roots + ((uint64_t)item * P.k + t) * N);
-            HF::t_absorb(ts, v, key);
-        }
         uint32_t o[W];
-        HF::t_final(o, ts);
+        slot_tl<HF>(slot, key, sk + 2 * N, pa, A.fors_roots + (uint64_t)item * P.k * N, P.k, o);
 #pragma unroll
         for (int x = 0; x < W; x++) forspk[x] = o[x];
         // the top layer root must equal the key's root; otherwise the key row

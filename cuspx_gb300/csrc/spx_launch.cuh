@@ -154,6 +154,7 @@ struct Family {
         if ((e = cudaFuncSetAttribute(k_verify_item<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_vsort_layer<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         if ((e = cudaFuncSetAttribute(k_vspec_walk<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
+        if ((e = cudaFuncSetAttribute(k_sign_finish<HF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))) return e;
         // Load every other kernel of the family now: with lazy module loading
         // a kernel's first launch loads it, and in a server that first launch
         // is a request's (one took ~50 ms of host time and held back every
@@ -235,7 +236,12 @@ struct Family {
             constexpr int LEN = 2 * N + 3;
             k_leaf_chains<HF><<<ceil_div(nleaves * LEN, 128), 128, 0, s>>>(P, L);
             CUSPX_MARK(pt, "k_leaf_chains", s);
-            k_leaf_tlen<HF><<<ceil_div(nleaves, 64), 64, (size_t)64 * HF::kSmemWords * 4, s>>>(P, L);
+            if (L.work) {   // signing: 32 threads per block, each with a slot of 1-5 KB
+                const uint32_t sw = VsortSmem<HF>::slot_stride(0);
+                k_leaf_tlen<HF><<<ceil_div(nleaves, 32), 32, (size_t)32 * sw * 4, s>>>(P, L, sw);
+            } else {
+                k_leaf_tlen<HF><<<ceil_div(nleaves, 64), 64, (size_t)64 * HF::kSmemWords * 4, s>>>(P, L, 0u);
+            }
             CUSPX_MARK(pt, "k_leaf_tlen", s);
             return;
         }
@@ -286,7 +292,7 @@ struct Family {
             CUSPX_MARK(pt, "k_trees", s);
         }
         if (split) cudaStreamWaitEvent(s, fk->join, 0);
-        k_sign_finish<HF><<<A.count, 128, (8 + HF::kSmemWords) * 4, s>>>(P, A);
+        k_sign_finish<HF><<<A.count, 128, (8 + VsortSmem<HF>::slot_stride(0)) * 4, s>>>(P, A);
         CUSPX_MARK(pt, "k_sign_finish", s);
     }
 

@@ -206,6 +206,53 @@ SPX_DEV void vslot_root(const SetParams &P, uint32_t *S, const SignWork &wk, con
     }
 }
 
+template <class HF>
+SPX_DEV void slot_tl(uint32_t *S, const KeyRegs<4 * HF::W> &key, const uint8_t *pub, const Adrs &pa,
+                     const uint8_t *vals, int m, uint32_t out[HF::W]) {
+    using PV = VerifyPolicy<HF>;
+    constexpr int NW = PV::N / 8, kBatch = 16;
+    uint32_t *stream = S + PV::S_HDR;
+    const uint2 *src = reinterpret_cast<const uint2 *>(vals);
+    const int vw = m * NW;
+    for (int q0 = 0; q0 < vw; q0 += kBatch) {
+        uint2 x[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; k++)
+            if (q0 + k < vw) x[k] = src[q0 + k];
+#pragma unroll
+        for (int k = 0; k < kBatch; k++)
+            if (q0 + k < vw) PV::put_value_word(stream, q0 + k, x[k]);
+    }
+    // key material as the policy lays it out (SHA-256: the PUB_SEED
+    // midstate, from a work record; SHAKE and robust SHA-256: PUB_SEED)
+    SignWork wk;
+#pragma unroll
+    for (int i = 0; i < 8; i++) wk.mid[i] = key.mid[i];
+    for (uint32_t l = 0; l < 32; l++) PV::load_key(S, &wk, pub, l);
+    for (uint32_t l = 0; l < 32; l++) PV::frame(stream, S, pa, m, l);
+    S[PV::S_M] = (uint32_t)m;
+    S[PV::S_NB] = (uint32_t)PV::stream_blocks(m);
+    S[PV::S_MASK] = S[PV::S_MASK + 1] = S[PV::S_MASK + 2] = ~0u;   // every value present
+    typename PV::LaneRegs lr{};
+    PV::claim_t(lr, S, 0);   // hp 0: no auth path in this slot
+    const int nbk = PV::stream_blocks(m);
+    for (int j = 0; j < nbk;) {
+        typename PV::Unit u;
+        if constexpr (PV::kTMask) {
+            if (PV::t_action(S, j) == 1) {
+                PV::build_mask(u, S, 0);
+                PV::run(u);
+                PV::after_mask(u, S, 0);
+                continue;
+            }
+        }
+        PV::build_t(u, lr, S, j, 0);
+        PV::run(u);
+        PV::after_t(u, lr, S, 0);
+        if (++j == nbk) PV::value_out(u, out);
+    }
+}
+
 // Thread per item of the group [first, first + n): the root of layer L (T_k
 // for L = -1), then either the verdict (L = d-1) or layer L+1's chains
 // bucketed by steps.  The block stages its items' values and auth paths into

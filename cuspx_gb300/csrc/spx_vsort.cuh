@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(32) k_vspec_walk(SetParams P, VerifyArgs A, co
     using PV = VerifyPolicy<HF>;
     using SM = VsortSmem<HF>;
     constexpr int W = PV::W, N = PV::N, LEN = PV::LEN, NW = N / 8;
-    constexpr int kBatch = 8;   // chain ends loaded before they are stored
+    constexpr int kBatch = 24 / NW;   // chain ends loaded before they are stored (24 8-byte words)
     extern __shared__ __align__(16) uint32_t smem[];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.count) return;   // no barriers in this kernel

@@ -120,6 +120,16 @@ def _time(batch, reps):
     return best
 
 
+def search_space(op, b):
+    """The knob values swept for `op` in batch-size bucket b (None in the
+    tables stands for b itself)."""
+    space = {k: [b if v is None else v for v in vals]
+             for k, vals in (SIGN_SPACE if op == OP_SIGN else VERIFY_SPACE).items()}
+    if "verify_spec_max" in space and b > SPEC_MAX_ITEMS:   # the speculative path covers up to 64 items
+        space["verify_spec_max"] = [0]
+    return space
+
+
 def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2, use_cache=True, verbose=False):
     """Pick the fastest mapping of `op` for set `sid` on a batch of `count`
     `mlen`-byte random messages, or on the given `msgs` (their count and
@@ -151,10 +161,7 @@ def tune(eng, sid, op=OP_SIGN, count=1024, mlen=64, msgs=None, reps=2, passes=2,
         vb = eng.batch(OP_VERIFY, sid, count, len(slab), 1)
         vb.upload(count, pks[0], 1, kidx, slab, len(slab), offs, lens, sigs)
         batch = vb
-    space = {k: [b if v is None else v for v in vals]
-             for k, vals in (SIGN_SPACE if op == OP_SIGN else VERIFY_SPACE).items()}
-    if "verify_spec_max" in space and b > SPEC_MAX_ITEMS:   # the speculative path covers up to 64 items
-        space["verify_spec_max"] = [0]
+    space = search_space(op, b)
     cur = {k: v for k, v in eng.get_tuning_for(sid, op, count).items() if k in space}
     eng.set_tuning_for(sid, op, *bucket_range(b), **cur)
     best_ms = _time(batch, reps)

@@ -182,3 +182,19 @@ def test_tuning_file_round_trip(tmp_path):
     assert sorted(tuple(x.split("\t")[3:5]) for x in lines) == [("257", "1024"), ("65", "256")]
     assert [autotune.bucket(n) for n in (1, 2, 4, 5, 64, 65, 4096)] == [1, 4, 4, 16, 64, 256, 4096]
     assert [autotune.bucket_range(b) for b in (1, 4, 64)] == [(1, 1), (2, 4), (17, 64)]
+
+
+def test_autotune_search_space():
+    """The verify search covers the sorted and speculative knobs; the
+    speculative size limit is only proposed where the library accepts it
+    (<= 64 items), and None entries become the bucket's size."""
+    import cuspx_gb300 as c
+    from cuspx_gb300 import autotune
+    small = autotune.search_space(c.OP_VERIFY, 16)
+    assert small["verify_spec_max"] == [0, 16] and small["verify_item_max"] == [0, 16]
+    assert 3 in small["verify_mode"] and small["verify_groups"] == [2, 4, 6, 8]
+    assert autotune.search_space(c.OP_VERIFY, 1024)["verify_spec_max"] == [0]
+    assert autotune.search_space(c.OP_VERIFY, 64)["verify_spec_max"] == [0, 64]
+    sign = autotune.search_space(c.OP_SIGN, 1024)
+    assert "verify_spec_max" not in sign and sign["chain_mode_max"] == [0, 256]
+    assert [autotune.bucket(n) for n in (1, 2, 5, 64, 65, 4096)] == [1, 4, 16, 64, 256, 4096]
